@@ -1,0 +1,750 @@
+// C ABI of libpypde_gb300.so: validation, launches, operator plans.
+//
+// Host-side factorisations (banded LU, offset-2 TDMA, per-eigenvalue Poisson
+// factors) happen once per plan in FP64 on the CPU; the device only ever
+// multiplies by stored reciprocals.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "pgx.h"
+
+namespace pgx {
+int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles);
+int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
+                   cudaStream_t s);
+}
+
+static thread_local int g_last_cuda = 0;
+
+static int cuda_fail(cudaError_t e) {
+  g_last_cuda = (int)e;
+  return PGX_E_CUDA;
+}
+#define PGX_CUDA(call)                          \
+  do {                                          \
+    cudaError_t e_ = (call);                    \
+    if (e_ != cudaSuccess) return cuda_fail(e_); \
+  } while (0)
+
+extern "C" const char* pgx_error_string(int code) {
+  switch (code) {
+    case PGX_OK: return "ok";
+    case PGX_E_ARG: return "invalid argument (shape, stride, length or enum)";
+    case PGX_E_CUDA: return "CUDA runtime error (see pgx_last_cuda_error)";
+    case PGX_E_SMEM: return "tile does not fit in shared memory";
+    case PGX_E_PLAN: return "null plan handle";
+    case PGX_E_SINGULAR: return "zero pivot in banded factorisation";
+    default: return "unknown pgx error";
+  }
+}
+extern "C" int pgx_last_cuda_error(void) { return g_last_cuda; }
+extern "C" int pgx_version(void) { return 1; }
+
+static int smem_optin_max() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (v <= 0) v = 48 * 1024;
+  }
+  return v;
+}
+
+static int check_program(const pgx_program* P) {
+  if (!P) return PGX_E_ARG;
+  if (P->axis < 0 || P->axis > 1 || P->tb < 1 || P->lcap < 1 || P->lcap > PGX_LMAX + 8) return PGX_E_ARG;
+  if (P->nslots < 1 || P->nslots > PGX_MAX_SLOTS || P->nops < 0 || P->nops > PGX_MAX_OPS) return PGX_E_ARG;
+  if (P->nthreads < 32 || P->nthreads > 1024 || (P->nthreads & 31)) return PGX_E_ARG;
+  if (P->lines_len < 0 || P->lines_len >= PGX_MAX_LEN) return PGX_E_ARG;
+  if (P->fft_n > P->lcap) return PGX_E_ARG;
+  for (int o = 0; o < P->nops; ++o) {
+    const pgx_op& op = P->ops[o];
+    if (op.a < 0 || op.a >= P->nslots) return PGX_E_ARG;
+    const bool uses_b = op.code == PGX_OP_AXPY || op.code == PGX_OP_MUL || op.code == PGX_OP_COPY;
+    if (uses_b && (op.b < 0 || op.b >= P->nslots)) return PGX_E_ARG;
+    if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;
+  }
+  int64_t need = pgx_program_smem(P) + 1024;
+  if (need > smem_optin_max()) return PGX_E_SMEM;
+  return PGX_OK;
+}
+
+// Checks the op arguments of a single instance against its lengths and arrays.
+static int check_instance(const pgx_program* P, const pgx_instance* I) {
+  int nl = I->len[P->lines_len];
+  if (nl < 0) return PGX_E_ARG;
+  for (int o = 0; o < P->nops; ++o) {
+    const pgx_op& op = P->ops[o];
+    switch (op.code) {
+      case PGX_OP_LOAD:
+      case PGX_OP_SETLEN:
+        if (op.len < 0 || I->len[op.len] < 0 || I->len[op.len] > P->lcap - 1) return PGX_E_ARG;
+        if (op.code == PGX_OP_SETLEN) break;
+        /* fallthrough */
+      case PGX_OP_LOAD_ADD:
+      case PGX_OP_LOAD_MUL:
+      case PGX_OP_STORE:
+      case PGX_OP_STORE_ADD: {
+        if (op.arr < 0) return PGX_E_ARG;
+        const pgx_array& a = I->arr[op.arr];
+        if (!a.ptr && (a.n0 > 0 && a.n1 > 0)) return PGX_E_ARG;
+        int ne = P->axis == 0 ? a.n0 : a.n1;
+        if (ne > P->lcap - 1) return PGX_E_ARG;
+        break;
+      }
+      case PGX_OP_DENSE:
+      case PGX_OP_BANDED:
+        if (op.mat < 0 || !I->mat[op.mat] || op.len < 0 || I->len[op.len] > P->lcap - 1) return PGX_E_ARG;
+        break;
+      case PGX_OP_STENCIL:
+      case PGX_OP_STENCIL_T:
+      case PGX_OP_TDMA2:
+      case PGX_OP_FDMA:
+      case PGX_OP_POISSON:
+      case PGX_OP_DCT:
+        if (op.mat < 0 || !I->mat[op.mat]) return PGX_E_ARG;
+        break;
+      default: break;
+    }
+  }
+  return PGX_OK;
+}
+
+extern "C" int pgx_run(const pgx_program* P, const pgx_instance* I, void* stream) {
+  int rc = check_program(P);
+  if (rc) return rc;
+  if (!I) return PGX_E_ARG;
+  rc = check_instance(P, I);
+  if (rc) return rc;
+  int nl = I->len[P->lines_len];
+  if (nl == 0) return PGX_OK;
+  int ntiles = (nl + P->tb - 1) / P->tb;
+  int e = pgx::launch_single(P, I, (cudaStream_t)stream, ntiles);
+  if (e) return cuda_fail((cudaError_t)e);
+  return PGX_OK;
+}
+
+extern "C" int pgx_run_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work,
+                               int32_t nwork, void* stream) {
+  int rc = check_program(P);
+  if (rc) return rc;
+  if (nwork < 0 || (nwork > 0 && (!d_insts || !d_work))) return PGX_E_ARG;
+  if (pgx_program_smem(P) + (int64_t)sizeof(pgx_instance) + 1024 > smem_optin_max()) return PGX_E_SMEM;
+  if (nwork == 0) return PGX_OK;
+  int e = pgx::launch_batched(P, d_insts, d_work, nwork, (cudaStream_t)stream);
+  if (e) return cuda_fail((cudaError_t)e);
+  return PGX_OK;
+}
+
+// ------------------------------------------------------------ device tables
+namespace {
+std::mutex g_mu;
+
+int upload(const std::vector<double>& h, double** d) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, h.size() * sizeof(double) + 16);
+  if (e != cudaSuccess) return cuda_fail(e);
+  e = cudaMemcpy(p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    return cuda_fail(e);
+  }
+  *d = (double*)p;
+  return PGX_OK;
+}
+
+bool fft_length_ok(int L) {
+  if (L < 2) return false;
+  while (L % 2 == 0) L /= 2;
+  while (L % 3 == 0) L /= 3;
+  return L == 1;
+}
+
+// key (device, n) -> twiddles exp(-2 pi i k / L), L = 2(n-1)
+std::map<std::pair<int, int>, double*> g_tw;
+// key (device, n, mode) -> dense scaled cosine matrix for lengths the FFT does not cover
+std::map<std::pair<int, int>, double*> g_dense;
+
+int device_id() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d;
+}
+
+int twiddles(int n, const double** out) {
+  int L = 2 * (n - 1);
+  if (!fft_length_ok(L)) return PGX_E_ARG;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_pair(device_id(), n);
+  auto it = g_tw.find(key);
+  if (it != g_tw.end()) {
+    *out = it->second;
+    return PGX_OK;
+  }
+  std::vector<double> h(2 * (size_t)L);
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < L; ++k) {
+    // reduce to the first octant for accuracy: angle = 2 pi k / L
+    double a = 2.0 * pi * (double)k / (double)L;
+    h[2 * k] = cos(a);
+    h[2 * k + 1] = -sin(a);
+  }
+  // exact values on the axes
+  for (int k = 0; k < L; ++k) {
+    if ((4 * k) % L == 0) {
+      int q = (4 * k) / L;
+      const double cs[4] = {1, 0, -1, 0}, sn[4] = {0, 1, 0, -1};
+      h[2 * k] = cs[q];
+      h[2 * k + 1] = -sn[q];
+    }
+  }
+  double* d = nullptr;
+  int rc = upload(h, &d);
+  if (rc) return rc;
+  g_tw[key] = d;
+  *out = d;
+  return PGX_OK;
+}
+
+// DCT-I as a dense matrix with the Chebyshev pre/post scaling folded in.
+int dense_dct(int n, int mode, const double** out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_pair(device_id(), n * 4 + mode);
+  auto it = g_dense.find(key);
+  if (it != g_dense.end()) {
+    *out = it->second;
+    return PGX_OK;
+  }
+  const int N = n - 1;
+  const double pi = 3.14159265358979323846;
+  std::vector<double> h((size_t)n * n);
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j) {
+      double c;
+      if (j == 0) c = 1.0;
+      else if (j == N) c = (k & 1) ? -1.0 : 1.0;
+      else {
+        long long r = ((long long)j * k) % (2 * N);  // cos(pi j k / N) with exact argument reduction
+        c = 2.0 * cos(pi * (double)r / (double)N);
+      }
+      if (mode == PGX_DCT_BWD) {
+        double s = (j == 0 || j == N) ? 1.0 : 0.5;
+        c *= (j & 1) ? -s : s;
+      } else if (mode == PGX_DCT_FWD) {
+        double s = (k == 0 || k == N) ? 0.5 / N : 1.0 / N;
+        c *= (k & 1) ? -s : s;
+      }
+      h[(size_t)k * n + j] = c;
+    }
+  double* d = nullptr;
+  int rc = upload(h, &d);
+  if (rc) return rc;
+  g_dense[key] = d;
+  *out = d;
+  return PGX_OK;
+}
+
+int round_odd(int x) { return x | 1; }
+
+// Lines per CTA and CTA size for a single-instance pass.
+void pick_tile(pgx_program* P, int nlines, int maxlen, int nbuf, int fft_n) {
+  P->lcap = round_odd(maxlen + 1);
+  int64_t per_line = (int64_t)8 * nbuf * P->lcap + (fft_n > 1 ? (int64_t)32 * (fft_n - 1) : 0);
+  int64_t budget = smem_optin_max() - 4096;
+  int tbmax = (int)(budget / per_line);
+  if (tbmax < 1) tbmax = 1;
+  int tb = (nlines + 151) / 152;
+  if (fft_n > 1 && tb < 2) tb = 2;
+  if (tb > 32) tb = 32;
+  if (tb > tbmax) tb = tbmax;
+  if (tb < 1) tb = 1;
+  P->tb = tb;
+  int work = tb * P->lcap / 2;
+  int nt = ((work + 31) / 32) * 32;
+  if (nt < 64) nt = 64;
+  if (nt > 512) nt = 512;
+  P->nthreads = nt;
+}
+
+pgx_op mk(int code, int a, int b = -1, int arr = -1, int mat = -1, int len = -1, int k = 0, double alpha = 1.0) {
+  pgx_op op;
+  op.code = (int16_t)code; op.a = (int16_t)a; op.b = (int16_t)b; op.arr = (int16_t)arr;
+  op.mat = (int16_t)mat; op.len = (int16_t)len; op.par = -1; op.k = (int16_t)k; op.alpha = alpha;
+  return op;
+}
+
+void set_arr(pgx_instance& I, int idx, const double* p, int64_t s0, int64_t s1, int n0, int n1) {
+  I.arr[idx].ptr = const_cast<double*>(p);
+  I.arr[idx].s0 = s0; I.arr[idx].s1 = s1; I.arr[idx].n0 = n0; I.arr[idx].n1 = n1;
+}
+
+// Array view (n_axis elements along `axis`, nlines lines) from pointer + strides.
+void set_axis_arr(pgx_instance& I, int idx, const double* p, int64_t s0, int64_t s1, int axis, int nel, int nlines) {
+  if (axis == 0) set_arr(I, idx, p, s0, s1, nel, nlines);
+  else set_arr(I, idx, p, s0, s1, nlines, nel);
+}
+
+void init_prog(pgx_program& P, pgx_instance& I, int axis) {
+  memset(&P, 0, sizeof(P));
+  memset(&I, 0, sizeof(I));
+  P.axis = axis;
+  P.lines_len = 0;
+  P.nslots = 1;
+}
+}  // namespace
+
+extern "C" int pgx_dct_table(int32_t n, const double** table) {
+  if (!table || n < 2 || n > PGX_LMAX - 8) return PGX_E_ARG;
+  return twiddles(n, table);
+}
+
+// ------------------------------------------------------------------- DCT-I
+extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, double* out, int64_t out_s0,
+                        int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
+                        void* stream) {
+  if (!in || !out || n < 2 || n > PGX_LMAX - 8 || n_in < 0 || n_in > n || n_out < 0 || n_out > n || nlines < 0 ||
+      axis < 0 || axis > 1 || mode < 0 || mode > 2)
+    return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = n;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, n_in, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, n_out, nlines);
+  const double* tab = nullptr;
+  bool fft = fft_length_ok(2 * (n - 1));
+  int rc = fft ? twiddles(n, &tab) : dense_dct(n, mode, &tab);
+  if (rc) return rc;
+  I.mat[0] = tab;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  if (fft) {
+    P.ops[1] = mk(PGX_OP_DCT, 0, -1, -1, 0, -1, mode);
+    P.fft_n = n;
+  } else {
+    P.ops[1] = mk(PGX_OP_DENSE, 0, -1, -1, 0, 1);
+  }
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, n, 2, P.fft_n);
+  return pgx_run(&P, &I, stream);
+}
+
+// ------------------------------------------------------- derivative recurrence
+extern "C" int pgx_cheb_diff(const double* c, int64_t c_s0, int64_t c_s1, double* dc, int64_t dc_s0, int64_t dc_s1,
+                             int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream) {
+  if (!c || !dc || n < 3 || n > PGX_LMAX - 8 || nlines < 0 || axis < 0 || axis > 1 || count < 0) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = n;
+  set_axis_arr(I, 0, c, c_s0, c_s1, axis, n, nlines);
+  set_axis_arr(I, 1, dc, dc_s0, dc_s1, axis, n, nlines);
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_DIFF, 0, -1, -1, -1, -1, count);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, n, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+// ---------------------------------------------------------------- stencils
+struct pgx_stencil_plan {
+  int N;
+  double* sub;    // S[i+2, i], i < N-2 (length N)
+  double* tdma;   // [aa | rden | w], each N-2
+};
+struct pgx_tdma_plan {
+  int n;
+  double* tab;
+};
+
+// Offset-2 TDMA table from diagonals a (n-2, offset -2), b (n), c (n-2, offset +2).
+static int tdma_table(const double* a, const double* b, const double* c, int n, std::vector<double>& tab) {
+  tab.assign(3 * (size_t)n, 0.0);
+  std::vector<double> w(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double den = i < 2 ? b[i] : b[i] - a[i - 2] * w[i - 2];
+    if (den == 0.0) return PGX_E_SINGULAR;
+    if (i < n - 2) w[i] = c[i] / den;
+    tab[n + i] = 1.0 / den;
+    tab[i] = i < 2 ? 0.0 : a[i - 2];
+  }
+  for (int i = 0; i < n; ++i) tab[2 * n + i] = w[i];
+  return PGX_OK;
+}
+
+extern "C" int pgx_stencil_plan_create(const char* key, int32_t N, pgx_stencil_plan** plan) {
+  if (!key || !plan || N < 5 || N > PGX_LMAX - 8) return PGX_E_ARG;
+  int kind;
+  if (!strcmp(key, "CD") || !strcmp(key, "ChebDirichlet")) kind = 0;
+  else if (!strcmp(key, "CN") || !strcmp(key, "ChebNeumann")) kind = 1;
+  else return PGX_E_ARG;
+  const int M = N - 2;
+  std::vector<double> sub(N, 0.0);
+  for (int i = 0; i < M; ++i) sub[i] = kind == 0 ? -1.0 : -((double)i / (i + 2)) * ((double)i / (i + 2));
+  // S^T S diagonals: d_i = 1 + s_i^2, off_{i,i+2} = s_i (S^T S is symmetric)
+  std::vector<double> a(M, 0.0), b(M, 0.0), c(M, 0.0);
+  for (int i = 0; i < M; ++i) b[i] = 1.0 + sub[i] * sub[i];
+  for (int i = 0; i + 2 < M; ++i) {
+    c[i] = sub[i];
+    a[i] = sub[i];
+  }
+  std::vector<double> tab;
+  int rc = tdma_table(a.data(), b.data(), c.data(), M, tab);
+  if (rc) return rc;
+  pgx_stencil_plan* p = new pgx_stencil_plan();
+  p->N = N;
+  rc = upload(sub, &p->sub);
+  if (!rc) rc = upload(tab, &p->tdma);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_stencil_plan_destroy(pgx_stencil_plan* p) {
+  if (!p) return PGX_E_PLAN;
+  cudaFree(p->sub);
+  cudaFree(p->tdma);
+  delete p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_stencil_to_chebyshev(const pgx_stencil_plan* p, const double* in, int64_t in_s0, int64_t in_s1,
+                                        double* out, int64_t out_s0, int64_t out_s1, int32_t nlines, int32_t axis,
+                                        void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!in || !out || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->N - 2;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, p->N - 2, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, p->N, nlines);
+  I.mat[0] = p->sub;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_STENCIL, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->N, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+extern "C" int pgx_stencil_from_chebyshev(const pgx_stencil_plan* p, const double* in, int64_t in_s0, int64_t in_s1,
+                                          double* out, int64_t out_s0, int64_t out_s1, int32_t nlines, int32_t axis,
+                                          void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!in || !out || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->N;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, p->N, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, p->N - 2, nlines);
+  I.mat[0] = p->sub;
+  I.mat[1] = p->tdma;
+  P.nops = 4;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_STENCIL_T, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_TDMA2, 0, -1, -1, 1);
+  P.ops[3] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->N, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+extern "C" int pgx_tdma_plan_create(const double* a, const double* b, const double* c, int32_t n, int32_t k,
+                                    pgx_tdma_plan** plan) {
+  if (!a || !b || !c || !plan || n < 3 || n > PGX_LMAX - 8 || k != 2) return PGX_E_ARG;
+  std::vector<double> tab;
+  int rc = tdma_table(a, b, c, n, tab);
+  if (rc) return rc;
+  pgx_tdma_plan* p = new pgx_tdma_plan();
+  p->n = n;
+  rc = upload(tab, &p->tab);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_tdma_plan_destroy(pgx_tdma_plan* p) {
+  if (!p) return PGX_E_PLAN;
+  cudaFree(p->tab);
+  delete p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_tdma_solve(const pgx_tdma_plan* p, const double* d, int64_t d_s0, int64_t d_s1, double* x,
+                              int64_t x_s0, int64_t x_s1, int32_t nlines, int32_t axis, void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!d || !x || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->n;
+  set_axis_arr(I, 0, d, d_s0, d_s1, axis, p->n, nlines);
+  set_axis_arr(I, 1, x, x_s0, x_s1, axis, p->n, nlines);
+  I.mat[0] = p->tab;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_TDMA2, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->n, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+// ------------------------------------------------------------------ FDMA
+struct pgx_fdma_plan {
+  int n;
+  double* tab;  // [l | dinv | u1 | u2]
+};
+
+static void fdma_tab(const double* l, const double* d, const double* u1, const double* u2, int n,
+                     std::vector<double>& tab, size_t off) {
+  for (int i = 0; i < n; ++i) {
+    tab[off + i] = (i >= 2 && l) ? l[i - 2] : 0.0;
+    tab[off + n + i] = 1.0 / d[i];
+    tab[off + 2 * n + i] = (i < n - 2 && u1) ? u1[i] : 0.0;
+    tab[off + 3 * n + i] = (i < n - 4 && u2) ? u2[i] : 0.0;
+  }
+}
+
+extern "C" int pgx_fdma_plan_create(const double* l, const double* d, const double* u1, const double* u2, int32_t n,
+                                    pgx_fdma_plan** plan) {
+  if (!d || !plan || n < 4 || n > PGX_LMAX - 8) return PGX_E_ARG;
+  for (int i = 0; i < n; ++i)
+    if (d[i] == 0.0) return PGX_E_SINGULAR;
+  std::vector<double> tab(4 * (size_t)n, 0.0);
+  fdma_tab(l, d, u1, u2, n, tab, 0);
+  pgx_fdma_plan* p = new pgx_fdma_plan();
+  p->n = n;
+  int rc = upload(tab, &p->tab);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_twodma_plan_create(const double* d, const double* u, int32_t n, pgx_fdma_plan** plan) {
+  return pgx_fdma_plan_create(nullptr, d, u, nullptr, n, plan);
+}
+
+extern "C" int pgx_fdma_plan_destroy(pgx_fdma_plan* p) {
+  if (!p) return PGX_E_PLAN;
+  cudaFree(p->tab);
+  delete p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_fdma_solve(const pgx_fdma_plan* p, double* x, int64_t s0, int64_t s1, int32_t nlines, int32_t axis,
+                              void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!x || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->n;
+  set_axis_arr(I, 0, x, s0, s1, axis, p->n, nlines);
+  I.mat[0] = p->tab;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_FDMA, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 0);
+  pick_tile(&P, nlines, p->n, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+// ---------------------------------------------------------------- Poisson
+struct pgx_poisson_plan {
+  int n, m;
+  double* tab;  // m lines x [l | dinv | u1 | u2] (n each)
+};
+
+// LU sweep of the four diagonals of an n x n band (init_fdma's recurrence).
+static int band_lu(std::vector<double>& l, std::vector<double>& d, std::vector<double>& u1, std::vector<double>& u2,
+                   int n) {
+  for (int i = 2; i < n; ++i) {
+    if (d[i - 2] == 0.0) return PGX_E_SINGULAR;
+    l[i - 2] = l[i - 2] / d[i - 2];
+    d[i] = d[i] - l[i - 2] * u1[i - 2];
+    if (i < n - 2) u1[i] = u1[i] - l[i - 2] * u2[i - 2];
+  }
+  for (int i = 0; i < n; ++i)
+    if (d[i] == 0.0) return PGX_E_SINGULAR;
+  return PGX_OK;
+}
+
+extern "C" int pgx_poisson_plan_create(const double* A, const double* C, const double* lam, int32_t n, int32_t m,
+                                       int32_t singular, pgx_poisson_plan** plan) {
+  if (!A || !C || !lam || !plan || n < 5 || n > PGX_LMAX - 8 || m < 1) return PGX_E_ARG;
+  std::vector<double> tab(4 * (size_t)n * m, 0.0);
+  for (int j = 0; j < m; ++j) {
+    const bool sing = singular && fabs(lam[j]) < 1e-10;
+    const int o = sing ? 1 : 0;  // solve rows/cols o: of A + lam C
+    const int ns = n - o;
+    std::vector<double> l(ns, 0.0), d(ns, 0.0), u1(ns, 0.0), u2(ns, 0.0);
+    auto el = [&](int r, int c) { return A[(size_t)(r + o) * n + c + o] + C[(size_t)(r + o) * n + c + o] * lam[j]; };
+    for (int i = 0; i < ns; ++i) {
+      d[i] = el(i, i);
+      if (i >= 2) l[i - 2] = el(i, i - 2);
+      if (i < ns - 2) u1[i] = el(i, i + 2);
+      if (i < ns - 4) u2[i] = el(i, i + 4);
+    }
+    int rc = band_lu(l, d, u1, u2, ns);
+    if (rc) return rc;
+    const size_t base = (size_t)j * 4 * n;
+    // place the ns-system at rows o..n-1 of a length-n table; row 0 of a singular
+    // line has dinv = 0 so the sweep yields x_0 = 0 (fdma.f90:176-179)
+    for (int i = 0; i < ns; ++i) {
+      int g = i + o;
+      tab[base + g] = i >= 2 ? l[i - 2] : 0.0;
+      tab[base + n + g] = 1.0 / d[i];
+      tab[base + 2 * n + g] = i < ns - 2 ? u1[i] : 0.0;
+      tab[base + 3 * n + g] = i < ns - 4 ? u2[i] : 0.0;
+    }
+  }
+  pgx_poisson_plan* p = new pgx_poisson_plan();
+  p->n = n;
+  p->m = m;
+  int rc = upload(tab, &p->tab);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_poisson_plan_destroy(pgx_poisson_plan* p) {
+  if (!p) return PGX_E_PLAN;
+  cudaFree(p->tab);
+  delete p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_poisson_solve(const pgx_poisson_plan* p, double* x, int64_t s0, int64_t s1, int32_t axis,
+                                 void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!x || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = p->m;
+  I.len[1] = p->n;
+  set_axis_arr(I, 0, x, s0, s1, axis, p->n, p->m);
+  I.mat[0] = p->tab;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_POISSON, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 0);
+  pick_tile(&P, p->m, p->n, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+// ----------------------------------------------------------------- matrices
+struct pgx_matrix_plan {
+  int rows, cols, banded, off0, ndiag;
+  double* tab;
+};
+
+extern "C" int pgx_matrix_plan_create(const double* A, int32_t rows, int32_t cols, pgx_matrix_plan** plan) {
+  if (!A || !plan || rows < 1 || cols < 1 || rows > PGX_LMAX - 8 || cols > PGX_LMAX - 8) return PGX_E_ARG;
+  int lo = 1 << 30, hi = -(1 << 30), parity = -1;
+  bool step2 = true;
+  for (int r = 0; r < rows; ++r)
+    for (int c = 0; c < cols; ++c)
+      if (A[(size_t)r * cols + c] != 0.0) {
+        int o = c - r;
+        if (o < lo) lo = o;
+        if (o > hi) hi = o;
+        int par = ((o % 2) + 2) % 2;
+        if (parity < 0) parity = par;
+        else if (par != parity) step2 = false;
+      }
+  pgx_matrix_plan* p = new pgx_matrix_plan();
+  p->rows = rows;
+  p->cols = cols;
+  std::vector<double> tab;
+  if (lo > hi) {  // all zero: one zero diagonal
+    lo = hi = 0;
+  }
+  int nd = (hi - lo) / 2 + 1;
+  if (step2 && nd <= 8) {
+    p->banded = 1;
+    p->off0 = lo;
+    p->ndiag = nd;
+    tab.assign((size_t)nd * rows, 0.0);
+    for (int d = 0; d < nd; ++d)
+      for (int r = 0; r < rows; ++r) {
+        int c = r + lo + 2 * d;
+        if (c >= 0 && c < cols) tab[(size_t)d * rows + r] = A[(size_t)r * cols + c];
+      }
+  } else {
+    p->banded = 0;
+    p->off0 = 0;
+    p->ndiag = 0;
+    tab.assign(A, A + (size_t)rows * cols);
+  }
+  int rc = upload(tab, &p->tab);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_matrix_plan_destroy(pgx_matrix_plan* p) {
+  if (!p) return PGX_E_PLAN;
+  cudaFree(p->tab);
+  delete p;
+  return PGX_OK;
+}
+
+extern "C" int pgx_matrix_plan_is_banded(const pgx_matrix_plan* p) { return p ? p->banded : 0; }
+
+extern "C" int pgx_matrix_apply(const pgx_matrix_plan* p, const double* in, int64_t in_s0, int64_t in_s1, double* out,
+                                int64_t out_s0, int64_t out_s1, int32_t nlines, int32_t axis, void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!in || !out || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->cols;
+  I.len[2] = p->rows;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, p->cols, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, p->rows, nlines);
+  I.mat[0] = p->tab;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  if (p->banded) {
+    P.ops[1] = mk(PGX_OP_BANDED, 0, p->off0, -1, 0, 2, p->ndiag);
+  } else {
+    P.ops[1] = mk(PGX_OP_DENSE, 0, -1, -1, 0, 2);
+  }
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->rows > p->cols ? p->rows : p->cols, 2, 0);
+  return pgx_run(&P, &I, stream);
+}

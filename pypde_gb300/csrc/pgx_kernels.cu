@@ -1,0 +1,589 @@
+// Line-program kernels for the pypde spectral-Galerkin time step on GB300 (sm_103a).
+//
+// One launch = one pass along one axis of a batch of 2-D arrays.  Every CTA owns
+// a tile of `tb` lines of one instance.  The lines are loaded into shared
+// memory "slots", a short program of 1-D operations (Chebyshev DCT-I via a
+// mixed-radix FFT, Shen stencils, derivative recurrence, banded / dense
+// operators, banded LU sweeps) runs on them, and results are stored back.
+//
+// All arithmetic is FP64.  On GB300 the FP64 pipe issues one warp instruction
+// per ~64 cycles per SM sub-partition (1.19 TFLOP/s for the whole GPU) and a
+// dependent DFMA has ~67 cycles of latency, so the kernels count FP64
+// instructions, never divide in inner loops (reciprocals come from host-built
+// tables), and keep index arithmetic in integer registers.
+//
+// Shared-memory invariant: every slot buffer holds zeros past the slot's
+// logical length up to `lcap`, so ops may read a few elements past the end
+// (banded sweeps read x[i+2], x[i+4]) without branches.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pgx.h"
+
+namespace pgx {
+
+// 2k for k < PGX_LMAX: multipliers of the derivative recurrence, read through
+// the constant cache (lanes of a warp read the same k in lockstep).
+struct TwoK {
+  double v[PGX_LMAX];
+};
+constexpr TwoK make_twok() {
+  TwoK t{};
+  for (int i = 0; i < PGX_LMAX; ++i) t.v[i] = 2.0 * i;
+  return t;
+}
+__constant__ TwoK c_twok = make_twok();
+
+struct Ctx {
+  double* sm;       // slot buffers
+  double2* f0;      // FFT ping buffer
+  double2* f1;      // FFT pong buffer
+  int tb, lcap, nthreads, tid;
+  int fft_stride;   // complex elements per pair in the FFT buffers
+  int l0, nlines;   // first line of the tile, lines of the instance
+  int phys[PGX_MAX_SLOTS + 1];
+  int slen[PGX_MAX_SLOTS];
+  int spare;
+};
+
+__device__ __forceinline__ double* slot_ptr(const Ctx& c, int s) {
+  return c.sm + (size_t)c.phys[s] * c.tb * c.lcap;
+}
+__device__ __forceinline__ double* spare_ptr(const Ctx& c) {
+  return c.sm + (size_t)c.spare * c.tb * c.lcap;
+}
+__device__ __forceinline__ void swap_spare(Ctx& c, int s) {
+  int t = c.phys[s];
+  c.phys[s] = c.spare;
+  c.spare = t;
+}
+
+__device__ __forceinline__ double op_alpha(const pgx_op& op, const pgx_instance& I) {
+  return op.par >= 0 ? op.alpha * I.par[op.par] : op.alpha;
+}
+
+// Geometry of array `a` seen from a pass along `axis`.
+struct View {
+  double* p;
+  int64_t se, sl;  // element stride, line stride
+  int ne, nl;      // elements per line, lines
+};
+__device__ __forceinline__ View view_of(const pgx_array& a, int axis) {
+  View v;
+  v.p = a.ptr;
+  if (axis == 0) {
+    v.se = a.s0; v.sl = a.s1; v.ne = a.n0; v.nl = a.n1;
+  } else {
+    v.se = a.s1; v.sl = a.s0; v.ne = a.n1; v.nl = a.n0;
+  }
+  return v;
+}
+
+// Zero [from, lcap) of every line of buffer `b`.
+__device__ void zero_tail(const Ctx& c, double* b, int from) {
+  int w = c.lcap - from;
+  if (w <= 0) return;
+  for (int idx = c.tid; idx < c.tb * w; idx += c.nthreads) {
+    int t = idx / w, i = from + idx % w;
+    b[t * c.lcap + i] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------ load/store
+// mode 0: slot = alpha*arr (length n, zero beyond the array), 1: +=, 2: *=
+__device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, int mode) {
+  const View v = view_of(I.arr[op.arr], axis);
+  const double alpha = op_alpha(op, I);
+  int n;
+  if (mode == 0) {
+    n = I.len[op.len];
+    c.slen[op.a] = n;
+  } else {
+    n = c.slen[op.a];
+  }
+  double* s = slot_ptr(c, op.a);
+  const int tb = c.tb;
+  const bool contig = (v.se == 1);
+  for (int idx = c.tid; idx < tb * n; idx += c.nthreads) {
+    int t, i;
+    if (contig) { t = idx / n; i = idx - t * n; }
+    else { i = idx / tb; t = idx - i * tb; }
+    const int line = c.l0 + t;
+    double x = 0.0;
+    if (i < v.ne && line < v.nl && line < c.nlines) x = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
+    double* d = s + t * c.lcap + i;
+    if (mode == 0) *d = alpha == 1.0 ? x : alpha * x;
+    else if (mode == 1) *d = fma(alpha, x, *d);
+    else *d = (alpha == 1.0 ? x : alpha * x) * (*d);
+  }
+  if (mode == 0) {
+    __syncthreads();
+    zero_tail(c, s, n);
+  }
+}
+
+__device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, bool add) {
+  const View v = view_of(I.arr[op.arr], axis);
+  const double alpha = op_alpha(op, I);
+  const double* s = slot_ptr(c, op.a);
+  const int n = v.ne;
+  const int tb = c.tb;
+  const bool contig = (v.se == 1);
+  for (int idx = c.tid; idx < tb * n; idx += c.nthreads) {
+    int t, i;
+    if (contig) { t = idx / n; i = idx - t * n; }
+    else { i = idx / tb; t = idx - i * tb; }
+    const int line = c.l0 + t;
+    if (line >= v.nl || line >= c.nlines) continue;
+    double x = s[t * c.lcap + i];
+    double* d = v.p + (int64_t)i * v.se + (int64_t)line * v.sl;
+    if (add) *d = fma(alpha, x, *d);
+    else *d = alpha == 1.0 ? x : alpha * x;
+  }
+}
+
+// ------------------------------------------------------------- pointwise ops
+__device__ void op_pointwise(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double alpha = op_alpha(op, I);
+  double* a = slot_ptr(c, op.a);
+  const double* b = op.b >= 0 ? slot_ptr(c, op.b) : nullptr;
+  int n = c.slen[op.a];
+  if (op.code != PGX_OP_SCALE) {
+    int nb = c.slen[op.b];
+    if (op.code == PGX_OP_COPY) n = nb;
+    else if (nb > n) n = nb;
+    c.slen[op.a] = n;
+  }
+  for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
+    int t = idx / n, i = idx - t * n;
+    int o = t * c.lcap + i;
+    switch (op.code) {
+      case PGX_OP_SCALE: a[o] *= alpha; break;
+      case PGX_OP_AXPY: a[o] = fma(alpha, b[o], a[o]); break;
+      case PGX_OP_MUL: a[o] = (alpha == 1.0 ? b[o] : alpha * b[o]) * a[o]; break;
+      case PGX_OP_COPY: a[o] = alpha == 1.0 ? b[o] : alpha * b[o]; break;
+    }
+  }
+  if (op.code == PGX_OP_COPY) {
+    __syncthreads();
+    zero_tail(c, a, n);
+  }
+}
+
+__device__ void op_setlen(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  int n = I.len[op.len];
+  int old = c.slen[op.a];
+  if (n < old) zero_tail(c, slot_ptr(c, op.a), n);
+  c.slen[op.a] = n;
+}
+
+// ------------------------------------------------------------------ stencils
+// u_i = v_i [i < M] + s_{i-2} v_{i-2} [i >= 2],  s = S[i+2, i] sub-diagonal table.
+__device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double* sd = I.mat[op.mat];
+  const double* x = slot_ptr(c, op.a);
+  double* y = spare_ptr(c);
+  const int M = c.slen[op.a], N = M + 2;
+  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
+    int t = idx / c.lcap, i = idx - t * c.lcap;
+    double r = 0.0;
+    if (i < N) {
+      const double* xl = x + t * c.lcap;
+      r = i < M ? xl[i] : 0.0;
+      if (i >= 2) r = fma(__ldg(sd + i - 2), xl[i - 2], r);
+    }
+    y[idx] = r;
+  }
+  swap_spare(c, op.a);
+  c.slen[op.a] = N;
+}
+
+// (S^T u)_i = u_i + s_i u_{i+2},  i < N-2.
+__device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double* sd = I.mat[op.mat];
+  const double* x = slot_ptr(c, op.a);
+  double* y = spare_ptr(c);
+  const int N = c.slen[op.a], M = N - 2;
+  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
+    int t = idx / c.lcap, i = idx - t * c.lcap;
+    double r = 0.0;
+    if (i < M) {
+      const double* xl = x + t * c.lcap;
+      r = fma(__ldg(sd + i), xl[i + 2], xl[i]);
+    }
+    y[idx] = r;
+  }
+  swap_spare(c, op.a);
+  c.slen[op.a] = M;
+}
+
+// ------------------------------------------------ sequential parity chains
+// Thread (t, p) owns the chain of line t with indices = p (mod 2).
+__device__ __forceinline__ bool chain_of(const Ctx& c, int& t, int& p) {
+  if (c.tid >= 2 * c.tb) return false;
+  p = c.tid / c.tb;
+  t = c.tid - p * c.tb;
+  return true;
+}
+
+// (S^T S) x = d with the offset-2 TDMA; table [aa | rden | w], each of length n:
+//   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}  (aa, w zero-padded).
+__device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  int t, p;
+  const int n = c.slen[op.a];
+  if (chain_of(c, t, p) && p < n) {
+    const double* tab = I.mat[op.mat];
+    const double* aa = tab;
+    const double* rden = tab + n;
+    const double* w = tab + 2 * n;
+    double* x = slot_ptr(c, op.a) + t * c.lcap;
+    double g = 0.0;
+    int i = p;
+    for (; i < n; i += 2) {
+      g = (x[i] - __ldg(aa + i) * g) * __ldg(rden + i);
+      x[i] = g;
+    }
+    double xn = 0.0;
+    for (i -= 2; i >= 0; i -= 2) {
+      xn = fma(-__ldg(w + i), xn, x[i]);
+      x[i] = xn;
+    }
+  }
+}
+
+// One Chebyshev derivative (differentiate_cheby.f90:28-53):
+//   dc_{n-1} = 0, dc_j = dc_{j+2} + 2(j+1) c_{j+1} (j = n-2..1), dc_0 = dc_2/2 + c_1.
+__device__ void op_diff_once(Ctx& c, int slot) {
+  const int n = c.slen[slot];
+  const double* x = slot_ptr(c, slot);
+  double* y = spare_ptr(c);
+  zero_tail(c, y, n - 1);
+  int t, p;
+  if (chain_of(c, t, p)) {
+    const double* xl = x + t * c.lcap;
+    double* yl = y + t * c.lcap;
+    int j = n - 2;
+    if ((j & 1) != p) --j;
+    double acc = 0.0;
+    for (; j >= 1; j -= 2) {
+      acc = fma(c_twok.v[j + 1], xl[j + 1], acc);
+      yl[j] = acc;
+    }
+    if (p == 0) yl[0] = fma(0.5, (n > 2 ? yl[2] : 0.0), xl[1]);
+  }
+  __syncthreads();
+  swap_spare(c, slot);
+}
+
+// In-place banded LU sweep for offsets -2, 0, +2, +4 (fdma.f90:1-38) with
+// factors [l | dinv | u1 | u2] (each n, zero-padded, l[i] couples x_i to x_{i-2}):
+//   forward  x_i -= l_i x_{i-2};   backward x_i = (x_i - u1_i x_{i+2} - u2_i x_{i+4}) dinv_i
+__device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, int p) {
+  const double* l = tab;
+  const double* dinv = tab + n;
+  const double* u1 = tab + 2 * n;
+  const double* u2 = tab + 3 * n;
+  double prev = x[p];
+  int i = p + 2;
+  for (; i < n; i += 2) {
+    prev = fma(-__ldg(l + i), prev, x[i]);
+    x[i] = prev;
+  }
+  double x2 = 0.0, x4 = 0.0;
+  for (i -= 2; i >= 0; i -= 2) {
+    double v = fma(-__ldg(u2 + i), x4, x[i]);
+    v = fma(-__ldg(u1 + i), x2, v) * __ldg(dinv + i);
+    x[i] = v;
+    x4 = x2;
+    x2 = v;
+  }
+}
+
+__device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line) {
+  int t, p;
+  const int n = c.slen[op.a];
+  if (chain_of(c, t, p) && p < n) {
+    const int line = c.l0 + t;
+    if (line < c.nlines) {
+      const double* tab = I.mat[op.mat];
+      if (per_line) tab += (size_t)line * 4 * n;
+      fdma_chain(slot_ptr(c, op.a) + t * c.lcap, tab, n, p);
+    }
+  }
+}
+
+// --------------------------------------------------------- banded / dense
+__device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double* A = I.mat[op.mat];
+  const int rows = I.len[op.len];
+  const int nd = op.k, off0 = op.b;
+  const int cols = c.slen[op.a];
+  const double* x = slot_ptr(c, op.a);
+  double* y = spare_ptr(c);
+  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
+    int t = idx / c.lcap, r = idx - t * c.lcap;
+    double acc = 0.0;
+    if (r < rows) {
+      const double* xl = x + t * c.lcap;
+      for (int d = 0; d < nd; ++d) {
+        int col = r + off0 + 2 * d;
+        if (col >= 0 && col < cols) acc = fma(__ldg(A + d * rows + r), xl[col], acc);
+      }
+    }
+    y[idx] = acc;
+  }
+  swap_spare(c, op.a);
+  c.slen[op.a] = rows;
+}
+
+__device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double* A = I.mat[op.mat];
+  const int rows = I.len[op.len];
+  const int cols = c.slen[op.a];
+  const double* x = slot_ptr(c, op.a);
+  double* y = spare_ptr(c);
+  zero_tail(c, y, rows);
+  for (int idx = c.tid; idx < c.tb * rows; idx += c.nthreads) {
+    int r = idx / c.tb, t = idx - r * c.tb;
+    const double* xl = x + t * c.lcap;
+    const double* Ar = A + (size_t)r * cols;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int k = 0;
+    for (; k + 3 < cols; k += 4) {
+      a0 = fma(__ldg(Ar + k), xl[k], a0);
+      a1 = fma(__ldg(Ar + k + 1), xl[k + 1], a1);
+      a2 = fma(__ldg(Ar + k + 2), xl[k + 2], a2);
+      a3 = fma(__ldg(Ar + k + 3), xl[k + 3], a3);
+    }
+    for (; k < cols; ++k) a0 = fma(__ldg(Ar + k), xl[k], a0);
+    y[t * c.lcap + r] = (a0 + a1) + (a2 + a3);
+  }
+  __syncthreads();
+  swap_spare(c, op.a);
+  c.slen[op.a] = rows;
+}
+
+// ---------------------------------------------------------------- DCT-I
+// DCT-I of two real lines at once: the even extensions e, e' (length L = 2(n-1))
+// form z = e + i e'; its DFT Z is y + i y' because the DFT of a real even
+// sequence is real.  The complex DFT is a mixed-radix (4, 2, 3) Stockham FFT in
+// shared memory; tw[k] = exp(-2 pi i k / L) comes from a host-built table.
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+template <int R>
+__device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src, double2* dst, const double2* tw,
+                                               int L, int Ns, int npairs) {
+  const int LR = L / R;
+  const int step = L / (Ns * R);
+  for (int idx = c.tid; idx < npairs * LR; idx += c.nthreads) {
+    int pr = idx / LR, j = idx - pr * LR;
+    const double2* s = src + pr * c.fft_stride;
+    double2* d = dst + pr * c.fft_stride;
+    int k = j % Ns;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[j + r * LR];
+    if (k != 0) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + k * r * step));
+    }
+    int base = (j - k) * R + k;
+    if (R == 2) {
+      d[base] = cadd(v[0], v[1]);
+      d[base + Ns] = csub(v[0], v[1]);
+    } else if (R == 4) {
+      double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+      double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
+      d[base] = cadd(a, e);
+      d[base + 2 * Ns] = csub(a, e);
+      // -i*f = (f.y, -f.x)
+      d[base + Ns] = make_double2(b.x + f.y, b.y - f.x);
+      d[base + 3 * Ns] = make_double2(b.x - f.y, b.y + f.x);
+    } else {  // R == 3, W3 = -1/2 - i sqrt(3)/2
+      const double h = 0.86602540378443864676;
+      double2 t1 = cadd(v[1], v[2]);
+      double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
+      double2 t3 = csub(v[1], v[2]);
+      d[base] = cadd(v[0], t1);
+      // out1 = t2 - i h t3 ; out2 = t2 + i h t3
+      d[base + Ns] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));
+      d[base + 2 * Ns] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));
+    }
+  }
+}
+
+__device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int n = c.slen[op.a];
+  const int N = n - 1, L = 2 * N;
+  const int mode = op.k;
+  const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
+  double* x = slot_ptr(c, op.a);
+  const int npairs = (c.tb + 1) >> 1;
+  // backward pre-scale: g_k = (-1)^k c_k, doubled at both ends, times the final 1/2
+  if (mode == PGX_DCT_BWD) {
+    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
+      int t = idx / n, k = idx - t * n;
+      double s = (k == 0 || k == N) ? 1.0 : 0.5;
+      x[t * c.lcap + k] *= (k & 1) ? -s : s;
+    }
+    __syncthreads();
+  }
+  // even extension of lines (2p, 2p+1) into z
+  for (int idx = c.tid; idx < npairs * L; idx += c.nthreads) {
+    int pr = idx / L, m = idx - pr * L;
+    int s = m <= N ? m : L - m;
+    int t0 = 2 * pr, t1 = t0 + 1;
+    double a = x[t0 * c.lcap + s];
+    double b = t1 < c.tb ? x[t1 * c.lcap + s] : 0.0;
+    c.f0[pr * c.fft_stride + m] = make_double2(a, b);
+  }
+  __syncthreads();
+  double2* src = c.f0;
+  double2* dst = c.f1;
+  int Ns = 1, rem = L;
+  while (rem > 1) {
+    if ((rem & 3) == 0) {
+      stockham_stage<4>(c, src, dst, tw, L, Ns, npairs);
+      Ns *= 4; rem >>= 2;
+    } else if ((rem & 1) == 0) {
+      stockham_stage<2>(c, src, dst, tw, L, Ns, npairs);
+      Ns *= 2; rem >>= 1;
+    } else {
+      stockham_stage<3>(c, src, dst, tw, L, Ns, npairs);
+      Ns *= 3; rem /= 3;
+    }
+    __syncthreads();
+    double2* tmp = src; src = dst; dst = tmp;
+  }
+  // output k = 0..N; forward post-scale: c_k = m_k (-1)^k y_k / (2N)
+  const double inv = (mode == PGX_DCT_FWD) ? 1.0 / N : 1.0;
+  for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
+    int t = idx / n, k = idx - t * n;
+    double2 z = src[(t >> 1) * c.fft_stride + k];
+    double y = (t & 1) ? z.y : z.x;
+    if (mode == PGX_DCT_FWD) {
+      double s = (k == 0 || k == N) ? 0.5 * inv : inv;
+      y *= (k & 1) ? -s : s;
+    }
+    x[t * c.lcap + k] = y;
+  }
+}
+
+// ------------------------------------------------------------------ driver
+template <bool BATCHED>
+__device__ void run_program(const pgx_program& P, const pgx_instance& I, int tile) {
+  extern __shared__ __align__(16) double smem_dyn[];
+  Ctx c;
+  c.tb = P.tb;
+  c.lcap = P.lcap;
+  c.nthreads = blockDim.x;
+  c.tid = threadIdx.x;
+  c.l0 = tile * P.tb;
+  c.nlines = I.len[P.lines_len];
+  const int nbuf = P.nslots + 1;
+  c.sm = BATCHED ? smem_dyn + (sizeof(pgx_instance) + 7) / 8 : smem_dyn;
+  size_t off = (size_t)nbuf * c.tb * c.lcap;
+  c.fft_stride = P.fft_n > 1 ? 2 * (P.fft_n - 1) : 0;
+  c.f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
+  c.f1 = c.f0 + (size_t)((c.tb + 1) >> 1) * c.fft_stride;
+  for (int s = 0; s < nbuf; ++s) c.phys[s] = s;
+  for (int s = 0; s < PGX_MAX_SLOTS; ++s) c.slen[s] = 0;
+  c.spare = P.nslots;
+  for (int s = 0; s < nbuf; ++s) {
+    double* b = c.sm + (size_t)s * c.tb * c.lcap;
+    for (int i = c.tid; i < c.tb * c.lcap; i += c.nthreads) b[i] = 0.0;
+  }
+  __syncthreads();
+  for (int o = 0; o < P.nops; ++o) {
+    const pgx_op& op = P.ops[o];
+    switch (op.code) {
+      case PGX_OP_LOAD: op_load(c, op, I, P.axis, 0); break;
+      case PGX_OP_LOAD_ADD: op_load(c, op, I, P.axis, 1); break;
+      case PGX_OP_LOAD_MUL: op_load(c, op, I, P.axis, 2); break;
+      case PGX_OP_STORE: op_store(c, op, I, P.axis, false); break;
+      case PGX_OP_STORE_ADD: op_store(c, op, I, P.axis, true); break;
+      case PGX_OP_SCALE:
+      case PGX_OP_AXPY:
+      case PGX_OP_MUL:
+      case PGX_OP_COPY: op_pointwise(c, op, I); break;
+      case PGX_OP_SETLEN: op_setlen(c, op, I); break;
+      case PGX_OP_STENCIL: op_stencil(c, op, I); break;
+      case PGX_OP_STENCIL_T: op_stencil_t(c, op, I); break;
+      case PGX_OP_TDMA2: op_tdma2(c, op, I); break;
+      case PGX_OP_DIFF:
+        for (int r = 0; r < op.k; ++r) op_diff_once(c, op.a);
+        break;
+      case PGX_OP_DCT: op_dct(c, op, I); break;
+      case PGX_OP_BANDED: op_banded(c, op, I); break;
+      case PGX_OP_DENSE: op_dense(c, op, I); break;
+      case PGX_OP_FDMA: op_fdma(c, op, I, false); break;
+      case PGX_OP_POISSON: op_fdma(c, op, I, true); break;
+      case PGX_OP_ZERO00:
+        if (c.l0 == 0 && c.tid == 0) slot_ptr(c, op.a)[0] = 0.0;
+        break;
+      default: break;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void line_program_single(const __grid_constant__ pgx_program P, const __grid_constant__ pgx_instance I) {
+  run_program<false>(P, I, blockIdx.x);
+}
+
+__global__ void line_program_batched(const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts,
+                                     const int32_t* __restrict__ work) {
+  extern __shared__ __align__(16) double smem_dyn[];
+  pgx_instance* sI = reinterpret_cast<pgx_instance*>(smem_dyn);
+  const int inst = work[2 * blockIdx.x], tile = work[2 * blockIdx.x + 1];
+  const int nwords = sizeof(pgx_instance) / 8;
+  const double* src = reinterpret_cast<const double*>(insts + inst);
+  double* dst = reinterpret_cast<double*>(sI);
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  run_program<true>(P, *sI, tile);
+}
+
+}  // namespace pgx
+
+// ---------------------------------------------------------------------------
+// Launch helpers used by the C ABI (pgx_api.cu).
+extern "C" int64_t pgx_program_smem(const pgx_program* P) {
+  int64_t nbuf = P->nslots + 1;
+  int64_t doubles = nbuf * P->tb * P->lcap;
+  doubles += doubles & 1;
+  if (P->fft_n > 1) doubles += 2 * 2 * (int64_t)((P->tb + 1) / 2) * 2 * (P->fft_n - 1);
+  return doubles * 8;
+}
+
+namespace pgx {
+int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles) {
+  int64_t smem = pgx_program_smem(P);
+  static thread_local int64_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaError_t e = cudaFuncSetAttribute(line_program_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    configured = smem;
+  }
+  line_program_single<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
+  return (int)cudaGetLastError();
+}
+
+int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
+                   cudaStream_t s) {
+  int64_t smem = pgx_program_smem(P) + ((sizeof(pgx_instance) + 15) / 16) * 16;
+  static thread_local int64_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaError_t e = cudaFuncSetAttribute(line_program_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    configured = smem;
+  }
+  line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  return (int)cudaGetLastError();
+}
+}  // namespace pgx

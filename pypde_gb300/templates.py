@@ -1,0 +1,83 @@
+"""Helmholtz / Poisson solver-plan templates (pypde/templates/{hholtz,poisson}.py)."""
+import numpy as np
+
+from .field import Field
+from .host import eigdecomp
+from .solver import PlanLHS, PlanRHS, SolverPlan
+
+
+def _axis_mats(base):
+    S = base.S
+    B = base.family.B(2, 2)
+    I = base.family.I(2)
+    return S, B, I
+
+
+def solverplan_hholtz1d(bases, lam):
+    """(1 - lam D2) u = rhs + uold, premultiplied by B (hholtz.py:4-39)."""
+    field = Field(bases)
+    assert field.ndim == 1
+    Sx, Bx, Ix = _axis_mats(field.xs[0])
+    Ax = Bx @ Sx - lam * Ix @ Sx
+    solver = SolverPlan()
+    solver.add_rhs(PlanRHS(Bx, ndim=1, axis=0))
+    solver.add_old(PlanRHS(Bx @ Sx, ndim=1, axis=0))
+    solver.add_lhs(PlanLHS(Ax, ndim=1, axis=0, method="fdma"))
+    return solver
+
+
+def solverplan_hholtz2d_adi(bases, lam, scale=(1, 1)):
+    """ADI-factored 2-D Helmholtz plan (hholtz.py:42-93)."""
+    field = Field(bases)
+    assert field.ndim == 2
+    solver = SolverPlan()
+    mats = []
+    for axis in range(2):
+        S, B, I = _axis_mats(field.xs[axis])
+        A = B @ S - lam * (1.0 / scale[axis] ** 2.0) * I @ S
+        mats.append((S, B, A))
+    for axis in range(2):
+        S, B, A = mats[axis]
+        solver.add_rhs(PlanRHS(B, ndim=2, axis=axis))
+        solver.add_old(PlanRHS(B @ S, ndim=2, axis=axis))
+        solver.add_lhs(PlanLHS(A, ndim=2, axis=axis, method="fdma"))
+    return solver
+
+
+def solverplan_poisson1d(bases, singular=False):
+    """D2 u = rhs premultiplied by B (poisson.py:4-40)."""
+    field = Field(bases)
+    assert field.ndim == 1
+    Sx, Bx, Ix = _axis_mats(field.xs[0])
+    Ax = Ix @ Sx
+    if singular:
+        assert Ax[0, 0] == 0, "Matrix does not look singular"
+        Ax[0, 0] += 1e-20
+    solver = SolverPlan()
+    solver.add_rhs(PlanRHS(Bx, ndim=1, axis=0))
+    solver.add_lhs(PlanLHS(Ax, ndim=1, axis=0, method="twodma"))
+    return solver
+
+
+def solverplan_poisson2d(bases, singular=False, scale=(1, 1)):
+    """Fast-diagonalisation 2-D Poisson plan (poisson.py:43-110)."""
+    field = Field(bases)
+    assert field.ndim == 2
+    Sx, Bx, Ix = _axis_mats(field.xs[0])
+    Ax = Ix @ Sx * (1.0 / scale[0] ** 2.0)
+    Cx = Bx @ Sx
+    Sy, By, Iy = _axis_mats(field.xs[1])
+    Ay = Iy @ Sy * (1.0 / scale[1] ** 2.0)
+    Cy = By @ Sy
+    CyI = np.linalg.inv(Cy)
+    wy, Qy, QyI = eigdecomp(CyI @ Ay)
+    if singular:
+        wy[0] += 1e-20
+    Hy = QyI @ CyI @ By
+    solver = SolverPlan()
+    solver.add_rhs(PlanRHS(Bx, ndim=2, axis=0))
+    solver.add_rhs(PlanRHS(Hy, ndim=2, axis=1))
+    solver.add_lhs(PlanLHS(Ax, alpha=wy, C=Cx, ndim=2, axis=0, method="poisson", singular=True))
+    solver.add_lhs(PlanLHS(Qy, ndim=2, axis=1, method="multiply"))
+    solver._fd = dict(Ax=Ax, Cx=Cx, wy=wy, Qy=Qy, Hy=Hy, Bx=Bx)
+    return solver

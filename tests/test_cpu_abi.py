@@ -1,0 +1,61 @@
+"""CPU checks of the product side: the C-ABI library builds, loads and exports every
+entry point include/pgx.h declares; ctypes mirrors match the C layouts; host-side
+setup matrices match the oracle.  No kernel is launched here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_err
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "pgx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pgx_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    from pypde_gb300 import build
+    lib = ctypes.CDLL(build.build())
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_header():
+    from pypde_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.SIGNATURES)
+
+
+def test_struct_layouts():
+    from pypde_gb300 import _lib
+    assert ctypes.sizeof(_lib.PgxArray) == 32
+    assert ctypes.sizeof(_lib.PgxOp) == 24
+    assert ctypes.sizeof(_lib.PgxInstance) == 832
+    assert ctypes.sizeof(_lib.PgxProgram) == 32 + 24 * 64
+
+
+def test_library_calls_without_gpu_are_safe():
+    from pypde_gb300 import _lib
+    L = _lib.lib()
+    assert L.pgx_version() == 1
+    assert L.pgx_error_string(1).startswith(b"invalid argument")
+    assert L.pgx_dct1(None, 1, 1, 5, None, 1, 1, 5, 5, 1, 0, 0, None) == 1
+
+
+@pytest.mark.parametrize("N", [17, 33, 65])
+def test_host_matrices_match_oracle(N):
+    from oracle import spectral as sp
+    from oracle import linalg as ol
+    from pypde_gb300 import host
+    assert np.array_equal(host.gauss_lobatto(N - 1), sp.gauss_lobatto(N - 1))
+    for key in ("CD", "CN", "DC", "NC"):
+        assert np.array_equal(host.stencil_matrix(key, N), sp.stencil(key, N))
+    assert rel_err(host.pseudoinverse_d2(N), sp.pseudoinverse_d2(N)) < 1e-15
+    A = sp.B2(N) @ sp.stencil("CD", N) - 0.01 * sp.I2(N) @ sp.stencil("CD", N)
+    for a, b in zip(host.fdma_lu(A), ol.fdma_factor(A)):
+        assert rel_err(a, b) < 1e-15
