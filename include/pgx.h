@@ -46,11 +46,11 @@ int pgx_version(void);
  * and stores results.  One launch = one pass along one axis.  The fused RBC
  * step and every single-operation entry point below are line programs.
  */
-#define PGX_MAX_ARR 16
+#define PGX_MAX_ARR 24
 #define PGX_MAX_MAT 16
 #define PGX_MAX_LEN 16
 #define PGX_MAX_PAR 16
-#define PGX_MAX_OPS 64
+#define PGX_MAX_OPS 96
 #define PGX_MAX_SLOTS 8
 #define PGX_LMAX 2112        /* longest line (elements) a program may hold */
 
@@ -80,7 +80,7 @@ enum pgx_opcode {
   PGX_OP_SETLEN = 10,   /* zero-pad / truncate slot a to len                 */
   PGX_OP_STENCIL = 11,  /* slot a (M) = S slot a (M+2); mat: S[i+2,i]        */
   PGX_OP_STENCIL_T = 12,/* slot a (N) = S^T slot a (N-2); mat: S[i+2,i]      */
-  PGX_OP_TDMA2 = 13,    /* slot a = (S^T S)^-1 slot a; mat: [a|rden|w]      */
+  PGX_OP_TDMA2 = 13,    /* slot a = (S^T S)^-1 slot a; mat: (a,rden,w) per i */
   PGX_OP_DIFF = 14,     /* slot a = D^k slot a (Chebyshev recurrence)        */
   PGX_OP_DCT = 15,      /* slot a = DCT-I slot a; k = mode; mat: twiddles    */
   PGX_OP_BANDED = 17,   /* slot a = A slot a; k diagonals from offset b step 2, rows len; mat [k][rows] */

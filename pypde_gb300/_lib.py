@@ -11,7 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpypde_gb300.so")
 
-MAX_ARR, MAX_MAT, MAX_LEN, MAX_PAR, MAX_OPS, MAX_SLOTS, LMAX = 16, 16, 16, 16, 64, 8, 2112
+MAX_ARR, MAX_MAT, MAX_LEN, MAX_PAR, MAX_OPS, MAX_SLOTS, LMAX = 24, 16, 16, 16, 96, 8, 2112
 
 OP = dict(LOAD=1, LOAD_ADD=2, LOAD_MUL=3, STORE=4, STORE_ADD=5, SCALE=6, AXPY=7, MUL=8, COPY=9,
           SETLEN=10, STENCIL=11, STENCIL_T=12, TDMA2=13, DIFF=14, DCT=15, BANDED=17, DENSE=18,
@@ -41,7 +41,7 @@ class PgxProgram(ctypes.Structure):
                 ("fft_n", ctypes.c_int32), ("nthreads", ctypes.c_int32), ("ops", PgxOp * MAX_OPS)]
 
 
-assert ctypes.sizeof(PgxInstance) == 832, ctypes.sizeof(PgxInstance)
+assert ctypes.sizeof(PgxInstance) == 32 * MAX_ARR + 8 * MAX_MAT + 4 * MAX_LEN + 8 * MAX_PAR
 assert ctypes.sizeof(PgxProgram) == 32 + 24 * MAX_OPS
 
 _lib = None

@@ -193,7 +193,6 @@ int twiddles(int n, const double** out) {
   std::vector<double> h(2 * (size_t)L);
   const double pi = 3.14159265358979323846;
   for (int k = 0; k < L; ++k) {
-    // reduce to the first octant for accuracy: angle = 2 pi k / L
     double a = 2.0 * pi * (double)k / (double)L;
     h[2 * k] = cos(a);
     h[2 * k + 1] = -sin(a);
@@ -362,14 +361,15 @@ extern "C" int pgx_cheb_diff(const double* c, int64_t c_s0, int64_t c_s1, double
 struct pgx_stencil_plan {
   int N;
   double* sub;    // S[i+2, i], i < N-2 (length N)
-  double* tdma;   // [aa | rden | w], each N-2
+  double* tdma;   // offset-2 TDMA factors, interleaved (a, rden, w) per index
 };
 struct pgx_tdma_plan {
   int n;
   double* tab;
 };
 
-// Offset-2 TDMA table from diagonals a (n-2, offset -2), b (n), c (n-2, offset +2).
+// Offset-2 TDMA table from diagonals a (n-2, offset -2), b (n), c (n-2, offset +2),
+// interleaved per index i: (a_{i-2}, 1/(b_i - a_{i-2} w_{i-2}), w_i).
 static int tdma_table(const double* a, const double* b, const double* c, int n, std::vector<double>& tab) {
   tab.assign(3 * (size_t)n, 0.0);
   std::vector<double> w(n, 0.0);
@@ -377,10 +377,10 @@ static int tdma_table(const double* a, const double* b, const double* c, int n, 
     double den = i < 2 ? b[i] : b[i] - a[i - 2] * w[i - 2];
     if (den == 0.0) return PGX_E_SINGULAR;
     if (i < n - 2) w[i] = c[i] / den;
-    tab[n + i] = 1.0 / den;
-    tab[i] = i < 2 ? 0.0 : a[i - 2];
+    tab[3 * i] = i < 2 ? 0.0 : a[i - 2];
+    tab[3 * i + 1] = 1.0 / den;
+    tab[3 * i + 2] = w[i];
   }
-  for (int i = 0; i < n; ++i) tab[2 * n + i] = w[i];
   return PGX_OK;
 }
 

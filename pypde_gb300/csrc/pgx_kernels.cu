@@ -227,26 +227,25 @@ __device__ __forceinline__ bool chain_of(const Ctx& c, int& t, int& p) {
   return true;
 }
 
-// (S^T S) x = d with the offset-2 TDMA; table [aa | rden | w], each of length n:
-//   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}  (aa, w zero-padded).
+// (S^T S) x = d with the offset-2 TDMA; table interleaved per index i as
+// (aa_i, rden_i, w_i), so one long table serves every system length n:
+//   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}.
+// The last two w_i of a chain multiply x_{n}, x_{n+1} = 0 and are never used.
 __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   int t, p;
   const int n = c.slen[op.a];
   if (chain_of(c, t, p) && p < n) {
     const double* tab = I.mat[op.mat];
-    const double* aa = tab;
-    const double* rden = tab + n;
-    const double* w = tab + 2 * n;
     double* x = slot_ptr(c, op.a) + t * c.lcap;
     double g = 0.0;
     int i = p;
     for (; i < n; i += 2) {
-      g = (x[i] - __ldg(aa + i) * g) * __ldg(rden + i);
+      g = (x[i] - __ldg(tab + 3 * i) * g) * __ldg(tab + 3 * i + 1);
       x[i] = g;
     }
     double xn = 0.0;
     for (i -= 2; i >= 0; i -= 2) {
-      xn = fma(-__ldg(w + i), xn, x[i]);
+      xn = fma(-__ldg(tab + 3 * i + 2), xn, x[i]);
       x[i] = xn;
     }
   }

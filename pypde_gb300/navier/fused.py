@@ -1,0 +1,601 @@
+"""Fused Rayleigh-Benard step: ten line-program passes per IMEX Euler step.
+
+The plain path (``NavierStokes.update``) launches one kernel per pypde
+operation (~150 launches per step).  Here the same step is regrouped into
+passes that each stream every array once through shared memory and chain all
+1-D operators along that axis: stencil, derivative recurrence, pad, DCT-I,
+pointwise products, forward DCT, unpad, pseudo-inverse B, four-diagonal LU
+sweep, ...  Operators acting along different axes commute, so x- and y-parts of
+the reference's sequence (rbc2d.py:396-434) are grouped per axis:
+
+  P1  x  S_x, D_x, pad, DCT^-1 of U, V, T          -> A_F0, A_Fx   (Nd x M-2)
+  P2  y  S_y, D_y, pad, DCT^-1; ux, uz; products;  -> C_F          (Nd x M)
+         forward DCT_y + unpad; D_y pres; S_y T
+  P3  x  forward DCT_x + unpad; rhs (pressure, buoyancy, BC terms); B_x;
+         A_x^-1 (ADI x-sweep); old terms B_x S_x F    -> Q1_F, Q2_F
+  P4  y  B_y Q1 + B_y S_y Q2; A_y^-1 -> U*, V*, T^{n+1}; S_y U*, D_y S_y V*
+  P5  x  divergence; pres -= nu div; B_x div              -> R1
+  P6  y  H_y (fast-diagonalisation rhs)                   -> R2
+  P7  x  per-eigenvalue Poisson sweep                     -> X
+  P8  y  Q_y, P[0,0] = 0; S_y P, D_y S_y P
+  P9  x  pres += S P / dt; grad P; (S^T S)^-1 S^T (x)     -> G1, G2
+  P10 y  (S^T S)^-1 S^T (y); U = U* - G1, V = V* - G2
+
+A batch of independent instances (any sizes, any Rayleigh numbers) runs the
+same ten launches: every CTA picks (instance, tile) from a work list, so one
+launch per pass covers all instances.  ``capture()`` records the passes of a
+step in a CUDA graph.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .._dev import DTYPE, device, stream, to_dev
+from ..host import fdma_lu, pseudoinverse_d2, stencil_matrix, stencil_sub
+
+# fixed len[] indices
+L_LINES, L_N, L_M, L_NG, L_MG, L_ND, L_MD = range(7)
+# fixed par[] indices
+P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT = range(9)
+
+FFT_RADICES = (2, 3)
+
+
+def fft_ok(n):
+    L = 2 * (n - 1)
+    for r in FFT_RADICES:
+        while L % r == 0 and L > 1:
+            L //= r
+    return L == 1
+
+
+class Prog:
+    """Builder of one line program with symbolic arrays and tables."""
+
+    def __init__(self, name, axis, lines, nslots):
+        self.name, self.axis, self.lines, self.nslots = name, axis, lines, nslots
+        self.ops, self.arrs, self.mats = [], {}, {}
+        self.has_dct = False
+
+    def _a(self, name):
+        return self.arrs.setdefault(name, len(self.arrs))
+
+    def _m(self, name):
+        return self.mats.setdefault(name, len(self.mats))
+
+    def add(self, code, a=0, b=-1, arr=None, mat=None, len=-1, k=0, alpha=1.0, par=-1):  # noqa: A002
+        self.ops.append(_lib.op(code, a=a, b=b, arr=-1 if arr is None else self._a(arr),
+                                mat=-1 if mat is None else self._m(mat), len=len, k=k, alpha=alpha, par=par))
+
+    # convenience
+    def load(self, s, arr, n, alpha=1.0, par=-1):
+        self.add("LOAD", s, arr=arr, len=n, alpha=alpha, par=par)
+
+    def load_add(self, s, arr, alpha=1.0, par=-1):
+        self.add("LOAD_ADD", s, arr=arr, alpha=alpha, par=par)
+
+    def store(self, s, arr):
+        self.add("STORE", s, arr=arr)
+
+    def stencil(self, s, kind):
+        self.add("STENCIL", s, mat="sten_" + kind)
+
+    def stencil_t(self, s, kind):
+        self.add("STENCIL_T", s, mat="sten_" + kind)
+
+    def tdma(self, s, kind):
+        self.add("TDMA2", s, mat="tdma_" + kind)
+
+    def diff(self, s, count=1):
+        self.add("DIFF", s, k=count)
+
+    def scale(self, s, alpha=1.0, par=-1):
+        self.add("SCALE", s, alpha=alpha, par=par)
+
+    def axpy(self, s, src, alpha=1.0, par=-1):
+        self.add("AXPY", s, b=src, alpha=alpha, par=par)
+
+    def mul(self, s, src):
+        self.add("MUL", s, b=src)
+
+    def copy(self, s, src):
+        self.add("COPY", s, b=src)
+
+    def setlen(self, s, n):
+        self.add("SETLEN", s, len=n)
+
+    def dct(self, s, mode, fft):
+        self.has_dct = True
+        if fft:
+            self.add("DCT", s, mat="dct", k=mode)
+        else:
+            self.add("DENSE", s, mat="dct_fwd" if mode == _lib.DCT_FWD else "dct_bwd", len=L_ND + self.axis)
+
+    def banded(self, s, name, off0, ndiag, rows):
+        self.add("BANDED", s, b=off0, mat=name, len=rows, k=ndiag)
+
+    def dense(self, s, name, rows):
+        self.add("DENSE", s, mat=name, len=rows)
+
+    def fdma(self, s, name):
+        self.add("FDMA", s, mat=name)
+
+
+def build_programs(tkind, fft):
+    """The ten passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
+    ("CD" for the linear / zero cases, "CN" for rbc)."""
+    P = []
+    BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
+    kinds = {"U": "CD", "V": "CD", "T": tkind}
+
+    # P1 (x, lines M-2): physical-in-x parts of F and dF/dx
+    p = Prog("P1", 0, L_MG, 2)
+    for F in "UVT":
+        p.load(0, F + "G", L_NG)
+        p.stencil(0, kinds[F])
+        p.copy(1, 0)
+        p.diff(1)
+        p.scale(1, par=P_ISX)
+        p.setlen(0, L_ND)
+        p.dct(0, BWD, fft)
+        p.store(0, "A_" + F + "0")
+        p.setlen(1, L_ND)
+        p.dct(1, BWD, fft)
+        p.store(1, "A_" + F + "x")
+    P.append(p)
+
+    # P2 (y, lines Nd): velocities, products, forward y-transform; D_y pres; S_y T
+    p = Prog("P2", 1, L_ND, 4)
+    for s, F in ((0, "U"), (1, "V")):
+        p.load(s, "A_" + F + "0", L_MG)
+        p.stencil(s, "CD")
+        p.setlen(s, L_MD)
+        p.dct(s, BWD, fft)
+    for F in "UVT":
+        p.load(2, "A_" + F + "x", L_MG)
+        p.stencil(2, "CD")
+        p.setlen(2, L_MD)
+        p.dct(2, BWD, fft)
+        p.mul(2, 0)
+        p.load(3, "A_" + F + "0", L_MG)
+        p.stencil(3, "CD")
+        p.diff(3)
+        p.scale(3, par=P_ISZ)
+        p.setlen(3, L_MD)
+        p.dct(3, BWD, fft)
+        p.mul(3, 1)
+        p.axpy(2, 3)
+        if F == "T":
+            p.load(3, "DTB1", L_MD)
+            p.mul(3, 1)
+            p.axpy(2, 3)
+        p.dct(2, FWD, fft)
+        p.setlen(2, L_M)
+        p.store(2, "C_" + F)
+    p.load(2, "PRES", L_M)
+    p.diff(2)
+    p.store(2, "DPZ")
+    p.load(2, "TG", L_MG)
+    p.stencil(2, "CD")
+    p.store(2, "TSY")
+    P.append(p)
+
+    # P3 (x, lines M): forward x-transform, right-hand sides, B_x, ADI x-sweep
+    p = Prog("P3", 0, L_M, 3)
+    for F in "UVT":
+        p.load(0, "C_" + F, L_ND)
+        p.dct(0, FWD, fft)
+        p.setlen(0, L_N)
+        p.scale(0, par=P_MDT)
+        if F == "U":
+            p.load(1, "PRES", L_N)
+            p.diff(1)
+            p.axpy(0, 1, par=P_MDTSX)
+        elif F == "V":
+            p.load_add(0, "DPZ", par=P_MDTSZ)
+            p.load_add(0, "TBCC", par=P_DT)
+            p.load(1, "TSY", L_NG)
+            p.stencil(1, tkind)
+            p.axpy(0, 1, par=P_DT)
+        else:
+            p.load_add(0, "DTB2", par=P_DTK)
+        p.banded(0, "Bx", 0, 3, L_NG)
+        p.fdma(0, "Ax_T" if F == "T" else "Ax_U")
+        p.store(0, "Q1_" + F)
+        p.load(2, F + "G", L_NG)
+        p.banded(2, "BSx_T" if F == "T" else "BSx_U", -2, 4, L_NG)
+        p.fdma(2, "Ax_T" if F == "T" else "Ax_U")
+        p.store(2, "Q2_" + F)
+    P.append(p)
+
+    # P4 (y, lines N-2): B_y, ADI y-sweep -> U*, V*, T; divergence pieces
+    p = Prog("P4", 1, L_NG, 3)
+    for F in "UVT":
+        p.load(0, "Q1_" + F, L_M)
+        p.banded(0, "By", 0, 3, L_MG)
+        p.load(1, "Q2_" + F, L_MG)
+        p.banded(1, "BSy", -2, 4, L_MG)
+        p.axpy(0, 1)
+        p.fdma(0, "Ay_T" if F == "T" else "Ay_U")
+        p.store(0, F + "G")
+        if F == "U":
+            p.stencil(0, "CD")
+            p.store(0, "W1")
+        elif F == "V":
+            p.stencil(0, "CD")
+            p.diff(0)
+            p.scale(0, par=P_ISZ)
+            p.store(0, "W2")
+    P.append(p)
+
+    # P5 (x, lines M): divergence, pres -= nu div, B_x div
+    p = Prog("P5", 0, L_M, 2)
+    p.load(0, "W1", L_NG)
+    p.stencil(0, "CD")
+    p.diff(0)
+    p.scale(0, par=P_ISX)
+    p.load(1, "W2", L_NG)
+    p.stencil(1, "CD")
+    p.axpy(0, 1)
+    p.load(1, "PRES", L_N)
+    p.axpy(1, 0, par=P_MNU)
+    p.store(1, "PRES")
+    p.banded(0, "Bx", 0, 3, L_NG)
+    p.store(0, "R1")
+    P.append(p)
+
+    # P6 (y, lines N-2): H_y
+    p = Prog("P6", 1, L_NG, 1)
+    p.load(0, "R1", L_M)
+    p.dense(0, "Hy", L_MG)
+    p.store(0, "R2")
+    P.append(p)
+
+    # P7 (x, lines M-2): per-eigenvalue four-diagonal sweep
+    p = Prog("P7", 0, L_MG, 1)
+    p.load(0, "R2", L_NG)
+    p.add("POISSON", 0, mat="Pois")
+    p.store(0, "X")
+    P.append(p)
+
+    # P8 (y, lines N-2): Q_y, P[0,0] = 0, S_y P, D_y S_y P
+    p = Prog("P8", 1, L_NG, 1)
+    p.load(0, "X", L_MG)
+    p.dense(0, "Qy", L_MG)
+    p.add("ZERO00", 0)
+    p.store(0, "PG")
+    p.stencil(0, "CN")
+    p.store(0, "Y1")
+    p.diff(0)
+    p.scale(0, par=P_ISZ)
+    p.store(0, "Y2")
+    P.append(p)
+
+    # P9 (x, lines M): pres += S_x S_y P / dt; grad P -> from_chebyshev along x
+    p = Prog("P9", 0, L_M, 2)
+    p.load(0, "Y1", L_NG)
+    p.stencil(0, "CN")
+    p.load(1, "PRES", L_N)
+    p.axpy(1, 0, par=P_IDT)
+    p.store(1, "PRES")
+    p.diff(0)
+    p.scale(0, par=P_ISX)
+    p.stencil_t(0, "CD")
+    p.tdma(0, "CD")
+    p.store(0, "G1")
+    p.load(1, "Y2", L_NG)
+    p.stencil(1, "CN")
+    p.stencil_t(1, "CD")
+    p.tdma(1, "CD")
+    p.store(1, "G2")
+    P.append(p)
+
+    # P10 (y, lines N-2): from_chebyshev along y, velocity correction
+    p = Prog("P10", 1, L_NG, 2)
+    for F, G in (("U", "G1"), ("V", "G2")):
+        p.load(0, G, L_M)
+        p.stencil_t(0, "CD")
+        p.tdma(0, "CD")
+        p.load(1, F + "G", L_MG)
+        p.axpy(1, 0, alpha=-1.0)
+        p.store(1, F + "G")
+    P.append(p)
+    return P
+
+
+_GLOBAL = {}
+
+
+def _global_tables():
+    """Length-independent device tables: stencil sub-diagonals and offset-2 TDMA factors.
+
+    For the Shen CD / CN stencils S[i+2, i] depends on i only, and so do the
+    forward factors of the TDMA on S^T S (the last two w_i of a shorter system
+    are never used by the sweep), so one long table serves every size.
+    """
+    dev = torch.cuda.current_device()
+    if dev in _GLOBAL:
+        return _GLOBAL[dev]
+    n = _lib.LMAX - 8
+    t = {}
+    for kind in ("CD", "CN"):
+        sub = stencil_sub(kind, n + 2)
+        t["sten_" + kind] = to_dev(np.concatenate([sub, np.zeros(2)]))
+        b = 1.0 + sub * sub
+        a = sub.copy()
+        c = sub.copy()
+        w = np.zeros(n)
+        rden = np.zeros(n)
+        aa = np.zeros(n)
+        for i in range(n):
+            den = b[i] if i < 2 else b[i] - a[i - 2] * w[i - 2]
+            w[i] = c[i] / den
+            rden[i] = 1.0 / den
+            aa[i] = 0.0 if i < 2 else a[i - 2]
+        t["tdma_" + kind] = (n, to_dev(np.stack([aa, rden, w], axis=1).ravel()))
+    _GLOBAL[dev] = t
+    return t
+
+
+def _banded_table(A, off0, ndiag):
+    rows, cols = A.shape
+    tab = np.zeros((ndiag, rows))
+    for d in range(ndiag):
+        for r in range(rows):
+            c = r + off0 + 2 * d
+            if 0 <= c < cols:
+                tab[d, r] = A[r, c]
+    # every nonzero of A must be on the stored diagonals
+    R = np.zeros_like(A)
+    for d in range(ndiag):
+        for r in range(rows):
+            c = r + off0 + 2 * d
+            if 0 <= c < cols:
+                R[r, c] = tab[d, r]
+    assert np.array_equal(R, A), "matrix is not banded on the expected diagonals"
+    return to_dev(tab.ravel())
+
+
+def _fdma_table(A):
+    l, d, u1, u2 = fdma_lu(A)
+    n = d.size
+    tab = np.zeros((4, n))
+    tab[0, 2:] = l
+    tab[1] = 1.0 / d
+    tab[2, :n - 2] = u1
+    tab[3, :n - 4] = u2
+    return to_dev(tab.ravel())
+
+
+def _poisson_table(Ax, Cx, lam):
+    """Per-eigenvalue LU factors of A + lam_j C with the singular rule (fdma.f90:146-185),
+    laid out [l | dinv | u1 | u2] per line; a singular line solves rows 1: and has dinv_0 = 0."""
+    n = Ax.shape[0]
+    m = lam.size
+    tab = np.zeros((m, 4, n))
+    for j in range(m):
+        o = 1 if abs(lam[j]) < 1e-10 else 0
+        A = (Ax + Cx * lam[j])[o:, o:]
+        l, d, u1, u2 = fdma_lu(A)
+        ns = n - o
+        tab[j, 0, o + 2:] = l
+        tab[j, 1, o:] = 1.0 / d
+        tab[j, 2, o:o + ns - 2] = u1
+        tab[j, 3, o:o + ns - 4] = u2
+    return to_dev(tab.ravel())
+
+
+def _dct_tables(n, fft):
+    if fft:
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().pgx_dct_table(n, ctypes.byref(h)), "dct table")
+        return {"dct": h.value}
+    N = n - 1
+    k = np.arange(n)[:, None]
+    j = np.arange(n)[None, :]
+    C = 2.0 * np.cos(np.pi * ((j * k) % (2 * N)) / N)
+    C[:, 0] = 1.0
+    C[:, -1] = (-1.0) ** np.arange(n)
+    pre = np.where((j == 0) | (j == N), 1.0, 0.5) * (-1.0) ** j
+    post = np.where((k == 0) | (k == N), 0.5 / N, 1.0 / N) * (-1.0) ** k
+    return {"dct_bwd": to_dev(C * pre), "dct_fwd": to_dev(C * post)}
+
+
+class _Instance:
+    """Device state, scratch and operator tables of one RBC instance."""
+
+    def __init__(self, ns, fft):
+        if ns.nstage != 1 or ns.beta != 1.0:
+            raise NotImplementedError("the fused step covers IMEX Euler with beta = 1; use update() otherwise")
+        self.ns = ns
+        N, M = ns.shape
+        Nd, Md = (int(1.5 * N), int(1.5 * M)) if ns.dealias else (N, M)
+        self.N, self.M, self.Nd, self.Md = N, M, Nd, Md
+        dev = device()
+        z = lambda r, c: torch.zeros((r, c), dtype=DTYPE, device=dev)  # noqa: E731
+        a = {}
+        # state (shared with the NavierStokes object's fields)
+        for key, fld in (("UG", ns.U), ("VG", ns.V), ("TG", ns.T), ("PG", ns.P), ("PRES", ns.pres)):
+            fld.vhat = a[key] = fld.vhat.contiguous()
+        a["TBCC"] = ns.Tbc_cheby.contiguous()
+        a["DTB1"] = ns.dTbcdz1.contiguous()
+        a["DTB2"] = ns.dTbcdz2.contiguous()
+        for F in "UVT":
+            a["A_" + F + "0"] = z(Nd, M - 2)
+            a["A_" + F + "x"] = z(Nd, M - 2)
+            a["C_" + F] = z(Nd, M)
+            a["Q1_" + F] = z(N - 2, M)
+            a["Q2_" + F] = z(N - 2, M - 2)
+        a["DPZ"] = z(N, M)
+        a["TSY"] = z(N - 2, M)
+        for k in ("W1", "W2", "R1", "Y1", "Y2", "G1", "G2"):
+            a[k] = z(N - 2, M)
+        a["R2"] = z(N - 2, M - 2)
+        a["X"] = z(N - 2, M - 2)
+        self.arrays = a
+        self.lens = [0, N, M, N - 2, M - 2, Nd, Md]
+        sx, sz = ns.scale
+        dt, nu, kap = ns.dt, ns.nu, ns.kappa
+        self.par = [1.0 / sx, 1.0 / sz, -dt, dt, dt * kap, -dt / sx, -dt / sz, -nu, 1.0 / dt]
+        # operator tables
+        g = _global_tables()
+        t = {"sten_CD": g["sten_CD"], "sten_CN": g["sten_CN"], "tdma_CD": g["tdma_CD"][1]}
+        tk = ns.T.xs[0].id
+        Bx, By = pseudoinverse_d2(N)[2:, :], pseudoinverse_d2(M)[2:, :]
+        Sx_U, Sx_T, Sy = stencil_matrix("CD", N), stencil_matrix(tk, N), stencil_matrix("CD", M)
+        t["Bx"] = _banded_table(Bx, 0, 3)
+        t["By"] = _banded_table(By, 0, 3)
+        t["BSx_U"] = _banded_table(Bx @ Sx_U, -2, 4)
+        t["BSx_T"] = _banded_table(Bx @ Sx_T, -2, 4)
+        t["BSy"] = _banded_table(By @ Sy, -2, 4)
+        Ix, Iy = np.eye(N)[2:, :], np.eye(M)[2:, :]
+        lu, lt = dt * nu, dt * kap
+        t["Ax_U"] = _fdma_table(Bx @ Sx_U - lu / sx ** 2 * Ix @ Sx_U)
+        t["Ax_T"] = _fdma_table(Bx @ Sx_T - lt / sx ** 2 * Ix @ Sx_T)
+        t["Ay_U"] = _fdma_table(By @ Sy - lu / sz ** 2 * Iy @ Sy)
+        t["Ay_T"] = _fdma_table(By @ Sy - lt / sz ** 2 * Iy @ Sy)
+        fd = ns.solver_P._fd
+        t["Pois"] = _poisson_table(np.asarray(fd["Ax"]), np.asarray(fd["Cx"]), np.real(fd["wy"]))
+        t["Hy"] = to_dev(np.ascontiguousarray(np.real(fd["Hy"])))
+        t["Qy"] = to_dev(np.ascontiguousarray(np.real(fd["Qy"])))
+        self.tables = t
+        self.dct_x = _dct_tables(Nd, fft)
+        self.dct_y = _dct_tables(Md, fft)
+
+    def sync_in(self):
+        """Point the solver's fields back at the fused state tensors (copying any newer values)."""
+        ns = self.ns
+        for key, fld in (("UG", ns.U), ("VG", ns.V), ("TG", ns.T), ("PG", ns.P), ("PRES", ns.pres)):
+            t = self.arrays[key]
+            if fld.vhat is not t:
+                t.copy_(fld.vhat)
+                fld.vhat = t
+
+    def lines(self, prog):
+        return self.lens[prog.lines] if prog.lines else 0
+
+    def fill(self, prog, inst):
+        """Resolve ``prog``'s symbolic arrays / tables for this instance into a PgxInstance."""
+        for name, idx in prog.arrs.items():
+            t = self.arrays[name]
+            A = inst.arr[idx]
+            A.ptr, A.s0, A.s1, A.n0, A.n1 = t.data_ptr(), t.stride(0), t.stride(1), t.shape[0], t.shape[1]
+        dct = self.dct_x if prog.axis == 0 else self.dct_y
+        for name, idx in prog.mats.items():
+            v = dct[name] if name.startswith("dct") else self.tables[name]
+            inst.mat[idx] = v if isinstance(v, int) else v.data_ptr()
+        for i, n in enumerate(self.lens):
+            inst.len[i] = n
+        inst.len[L_LINES] = self.lens[prog.lines]
+        for i, v in enumerate(self.par):
+            inst.par[i] = v
+
+
+def _pick(lines_total, lcap, nbuf, fft_n, max_lines):
+    """Lines per CTA and threads for a pass over ``lines_total`` lines (all instances)."""
+    per_line = 8 * nbuf * lcap + (32 * (fft_n - 1) if fft_n > 1 else 0)
+    budget = 200 * 1024 - 1024
+    tbmax = max(1, budget // per_line)
+    tb = max(1, -(-lines_total // (2 * 152)))
+    if fft_n > 1:
+        tb = max(tb, 2)
+    tb = min(tb, tbmax, 32, max(max_lines, 1))
+    if fft_n > 1 and tb > 1 and tb % 2:
+        tb -= 1
+    work = tb * lcap
+    nt = min(512, max(64, 32 * -(-work // (32 * 2))))
+    return tb, nt
+
+
+class FusedBatch:
+    """Fused Euler step for a batch of NavierStokes instances (any sizes / Ra)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        tkinds = {ns.T.xs[0].id for ns in self.solvers}
+        if len(tkinds) != 1:
+            raise ValueError("all instances of a batch need the same temperature basis")
+        sizes = [(int(1.5 * ns.shape[0]), int(1.5 * ns.shape[1])) if ns.dealias else ns.shape for ns in self.solvers]
+        self.fft = all(fft_ok(n) for s in sizes for n in s)
+        self.insts = [_Instance(ns, self.fft) for ns in self.solvers]
+        self.progs = build_programs(tkinds.pop(), self.fft)
+        self._build_launches()
+        self.graph = None
+
+    def _build_launches(self):
+        dev = device()
+        self.launches = []
+        for prog in self.progs:
+            lines = [I.lines(prog) for I in self.insts]
+            maxlen = 0
+            for I in self.insts:
+                lens = I.lens
+                m = max(lens[L_ND], lens[L_N]) if prog.axis == 0 else max(lens[L_MD], lens[L_M])
+                maxlen = max(maxlen, m)
+            lcap = (maxlen + 1) | 1
+            fft_n = maxlen if (prog.has_dct and self.fft) else 0
+            tb, nt = _pick(sum(lines), lcap, prog.nslots + 1, fft_n, max(lines))
+            P = _lib.PgxProgram()
+            P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
+            P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
+            assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
+            for i, o in enumerate(prog.ops):
+                P.ops[i] = o
+            insts = (_lib.PgxInstance * len(self.insts))()
+            for k, I in enumerate(self.insts):
+                I.fill(prog, insts[k])
+            d_insts = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(dev)
+            work = []
+            for k, nl in enumerate(lines):
+                work += [(k, t) for t in range(-(-nl // tb))]
+            d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=dev)
+            self.launches.append((prog.name, P, d_insts, d_work, len(work)))
+
+    def run_pass(self, i):
+        name, P, d_insts, d_work, nwork = self.launches[i]
+        _lib.check(_lib.lib().pgx_run_batched(ctypes.byref(P), d_insts.data_ptr(), d_work.data_ptr(), nwork,
+                                              stream()), name)
+
+    def step_eager(self):
+        for i in range(len(self.launches)):
+            self.run_pass(i)
+
+    def capture(self, nsteps=1):
+        """Record ``nsteps`` fused steps in a CUDA graph; ``step()`` then replays it."""
+        # the passes update the state in place: keep a copy, warm up once outside the
+        # capture (kernel attributes, lazy tables), restore, then record
+        saved = [{k: I.arrays[k].clone() for k in ("UG", "VG", "TG", "PG", "PRES")} for I in self.insts]
+        self.step_eager()
+        torch.cuda.synchronize()
+        for I, s in zip(self.insts, saved):
+            for k, v in s.items():
+                I.arrays[k].copy_(v)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(nsteps):
+                self.step_eager()
+        torch.cuda.synchronize()
+        for I, s in zip(self.insts, saved):
+            for k, v in s.items():
+                I.arrays[k].copy_(v)
+        self.graph, self.graph_steps = g, nsteps
+
+    def step(self):
+        """One fused step (graph replay when captured with nsteps == 1)."""
+        if self.graph is not None and self.graph_steps == 1:
+            self.graph.replay()
+        else:
+            self.step_eager()
+
+    @property
+    def launches_per_step(self):
+        return len(self.launches)
+
+
+class FusedStep(FusedBatch):
+    """Fused step of a single NavierStokes instance."""
+
+    def __init__(self, ns):
+        FusedBatch.__init__(self, [ns])

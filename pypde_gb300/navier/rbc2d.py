@@ -267,10 +267,16 @@ class NavierStokes(NavierStokesBase, Integrator):
 
     # ---------------------------------------------------------- fused step
     def fused(self):
-        """The fused line-program step for this configuration (built once)."""
+        """The fused line-program step for this configuration (built once).
+
+        The fused passes update the state tensors in place; if the plain path
+        (or the user) rebound ``vhat`` since, the current state is copied in.
+        """
         if self._fused is None:
             from .fused import FusedStep
             self._fused = FusedStep(self)
+        else:
+            self._fused.insts[0].sync_in()
         return self._fused
 
     def update_fused(self, nsteps=1):

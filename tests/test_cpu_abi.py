@@ -35,8 +35,8 @@ def test_struct_layouts():
     from pypde_gb300 import _lib
     assert ctypes.sizeof(_lib.PgxArray) == 32
     assert ctypes.sizeof(_lib.PgxOp) == 24
-    assert ctypes.sizeof(_lib.PgxInstance) == 832
-    assert ctypes.sizeof(_lib.PgxProgram) == 32 + 24 * 64
+    assert ctypes.sizeof(_lib.PgxInstance) == 32 * 24 + 8 * 16 + 4 * 16 + 8 * 16
+    assert ctypes.sizeof(_lib.PgxProgram) == 32 + 24 * 96
 
 
 def test_library_calls_without_gpu_are_safe():
@@ -59,3 +59,26 @@ def test_host_matrices_match_oracle(N):
     A = sp.B2(N) @ sp.stencil("CD", N) - 0.01 * sp.I2(N) @ sp.stencil("CD", N)
     for a, b in zip(host.fdma_lu(A), ol.fdma_factor(A)):
         assert rel_err(a, b) < 1e-15
+
+
+@pytest.mark.parametrize("tkind", ["CD", "CN"])
+@pytest.mark.parametrize("fft", [True, False])
+def test_fused_programs_fit_the_abi(tkind, fft):
+    """Every fused pass respects the C-ABI limits and uses only slots it declares."""
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import build_programs
+    progs = build_programs(tkind, fft)
+    assert len(progs) == 10
+    uses_b = {_lib.OP[k] for k in ("AXPY", "MUL", "COPY")}
+    for p in progs:
+        assert len(p.ops) <= _lib.MAX_OPS, p.name
+        assert len(p.arrs) <= _lib.MAX_ARR, p.name
+        assert len(p.mats) <= _lib.MAX_MAT, p.name
+        assert 1 <= p.nslots <= _lib.MAX_SLOTS
+        for o in p.ops:
+            assert 0 <= o.a < p.nslots, p.name
+            if o.code in uses_b:
+                assert 0 <= o.b < p.nslots, p.name
+            assert o.len < _lib.MAX_LEN and o.par < _lib.MAX_PAR
+        # every array stored is either state or scratch; every loaded array is defined
+        assert p.axis in (0, 1)

@@ -1,0 +1,126 @@
+"""GPU parity of the fused line-program step (single instance, CUDA graph, batches).
+
+Tolerances: 1e-9 relative on states after one step, 1e-8 after many steps and
+on Nusselt number / kinetic energy (the path's stated target after 100 steps).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def NS():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from pypde_gb300.navier.rbc2d import NavierStokes
+    return NavierStokes
+
+
+def oracle_run(case, shape, cfg, seed, amp, nsteps):
+    from oracle import rbc2d as orb
+    ref = orb.NavierStokes(case=case, shape=shape, pr=1.0, tsave=None, **cfg)
+    orb.seeded_temperature(ref, seed, amp)
+    for _ in range(nsteps):
+        ref.update()
+    return ref
+
+
+def compare(ns, ref, tol):
+    st = ns.state()
+    for name, arr in (("T", ref.That), ("U", ref.Uhat), ("V", ref.Vhat), ("P", ref.Phat), ("pres", ref.pres)):
+        e = rel_err(st[name], arr)
+        assert e < tol, (name, e)
+
+
+CASES = [
+    ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
+    ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=False)),
+    ("linear", (33, 17), dict(ra=3e4, dt=0.01, dealias=True, aspect=2.0)),
+    ("rbc", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
+    ("zero", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
+    ("linear", (65, 33), dict(ra=1e6, dt=0.005, dealias=True)),
+    ("linear", (40, 24), dict(ra=1e5, dt=0.01, dealias=True)),   # 59, 35: dense DCT fallback
+]
+
+
+@pytest.mark.parametrize("case,shape,cfg", CASES, ids=[f"{c[0]}-{c[1][0]}x{c[1][1]}-{i}" for i, c in enumerate(CASES)])
+def test_fused_vs_oracle(NS, case, shape, cfg):
+    ns = NS(case=case, shape=shape, pr=1.0, tsave=None, integrator="eu", **cfg)
+    ns.set_temperature_noise(7, 1e-2)
+    f = ns.fused()
+    f.step_eager()
+    compare(ns, oracle_run(case, shape, cfg, 7, 1e-2, 1), 1e-9)
+    for _ in range(9):
+        f.step_eager()
+    compare(ns, oracle_run(case, shape, cfg, 7, 1e-2, 10), 1e-8)
+
+
+def test_fused_c1_100_steps_golden(NS, golden):
+    """The 65x65, Ra 1e5, dt 0.01 case: Nu, Nuvol and KE after 100 steps within 1e-8 of the reference."""
+    ns = NS(case="linear", shape=(65, 65), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", tsave=None)
+    ns.set_temperature_noise(0, 1e-3)
+    f = ns.fused()
+    f.capture(1)
+    for _ in range(100):
+        f.step()
+    st = ns.state()
+    for name in ("T", "U", "V", "P", "pres"):
+        assert rel_err(st[name], golden[f"rbc_c1_s100_{name}"]) < 1e-8, name
+    nu, nuv, ke = golden["rbc_c1_s100_scalars"]
+    Nu, Nuv = ns.eval_Nu()
+    assert abs(Nu - nu) / abs(nu) < 1e-8
+    assert abs(Nuv - nuv) / abs(nuv) < 1e-8
+    assert abs(ns.eval_KE() - ke) / abs(ke) < 1e-8
+
+
+def test_graph_replay_equals_eager(NS):
+    import torch
+    kw = dict(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", tsave=None)
+    a, b = NS(**kw), NS(**kw)
+    a.set_temperature_noise(3, 1e-2)
+    b.set_temperature_noise(3, 1e-2)
+    fa, fb = a.fused(), b.fused()
+    fb.capture(1)
+    for _ in range(5):
+        fa.step_eager()
+        fb.step()
+    torch.cuda.synchronize()
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_fused_matches_plain(NS):
+    kw = dict(case="rbc", shape=(33, 49), ra=2e5, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+    a, b = NS(**kw), NS(**kw)
+    a.set_temperature_noise(4, 1e-2)
+    b.set_temperature_noise(4, 1e-2)
+    for _ in range(5):
+        a.update()
+    b.update_fused(5)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        assert rel_err(sb[k], sa[k]) < 1e-9, k
+
+
+def test_batched_heterogeneous(NS):
+    """Instances of different sizes and Rayleigh numbers in one batch, each vs its own oracle."""
+    from pypde_gb300.navier.fused import FusedBatch
+    specs = [((33, 33), 1e4, 100), ((65, 33), 1e5, 101), ((33, 129), 3e6, 102), ((129, 65), 1e7, 103),
+             ((65, 65), 5e5, 104)]
+    solvers = []
+    for shape, ra, seed in specs:
+        ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+        ns.set_temperature_noise(seed, 1e-3)
+        solvers.append(ns)
+    fb = FusedBatch(solvers)
+    fb.capture(1)
+    for _ in range(3):
+        fb.step()
+    for ns, (shape, ra, seed) in zip(solvers, specs):
+        ref = oracle_run("linear", shape, dict(ra=ra, dt=0.005, dealias=True), seed, 1e-3, 3)
+        compare(ns, ref, 1e-8)
