@@ -1,0 +1,442 @@
+"""Benchmark: batched 2-D Rayleigh-Benard FP64 time steps on one GB300.
+
+Workload (default, the batched configuration the headline metric is quoted
+on): 256 independent RBC instances, Nx and Ny drawn iid from {33, 65, 129}
+(numpy default_rng(99)), Ra log-uniform in [1e4, 1e7] (same generator),
+Pr = 1, aspect 1, dt = 0.005, IMEX Euler, 3/2 dealiasing, case "linear",
+T = conductive profile + 1e-3 U(-1,1) noise with seed 100 + i.
+
+A step = one time step of every instance (all 256), replayed from one CUDA
+graph of ten fused line-program launches.  ``value`` = instance-steps/s with
+the state resident in HBM; ``e2e`` = the same through the public API with the
+state in pinned host memory (one H2D copy of every instance's state before and
+one D2H copy after each step, inside the timed region).  ``plain`` = the same
+instances run one by one on the per-instance GPU path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--instances 256] [--workload c4|c1|c3]
+Under torchrun every rank runs its own batch (weak scaling, no collective on
+the data path); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "2D RBC FP64 steps/s at 1 GB300: plain vs batched-graph; adjoint grads/s at 1e-6 rel"
+FP64_PEAK_TFLOPS = 1.19  # measured DFMA throughput of this GB300 (profiles/gb300_fp64_probe.txt)
+
+
+def workload_specs(kind, n_instances, rank=0):
+    """(shape, ra, dt, seed, amplitude, aspect) for every instance of the workload."""
+    if kind == "c4":
+        rng = np.random.default_rng(99)
+        sizes = rng.choice([33, 65, 129], size=(n_instances * (rank + 1), 2))[n_instances * rank:]
+        ras = 10.0 ** rng.uniform(4.0, 7.0, n_instances * (rank + 1))[n_instances * rank:]
+        return [((int(a), int(b)), float(ra), 0.005, 100 + n_instances * rank + i, 1e-3, 1.0)
+                for i, ((a, b), ra) in enumerate(zip(sizes, ras))]
+    if kind == "c1":
+        return [((65, 65), 1e5, 0.01, 0, 1e-3, 1.0)]
+    if kind == "c3":
+        return [((513, 257), 1e8, 1e-3, 2, 1e-3, 2.0)]
+    raise ValueError(kind)
+
+
+WORKLOAD_NAMES = {
+    "c4": "batched 2D RBC: {n} instances, Nx,Ny iid {{33,65,129}}, Ra log-uniform [1e4,1e7], Pr 1, dt 0.005",
+    "c1": "plain 2D RBC 65x65, Ra 1e5, Pr 1, dt 0.01",
+    "c3": "large plain 2D RBC 513x257, aspect 2, Ra 1e8, Pr 1, dt 1e-3",
+}
+
+
+# ------------------------------------------------------------------ CPU side
+_WORKER = {}
+BLAS_ENV = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+def _oracle_init(specs):
+    sys.path.insert(0, ROOT)
+    from oracle import rbc2d as orb
+    sols = []
+    for shape, ra, dt, seed, amp, aspect in specs:
+        ns = orb.NavierStokes(case="linear", shape=shape, ra=ra, pr=1.0, dt=dt, aspect=aspect, dealias=True,
+                              integrator="eu", beta=1.0, tsave=None)
+        orb.seeded_temperature(ns, seed, amp)
+        sols.append(ns)
+    _WORKER["sols"] = sols
+
+
+def _oracle_steps(steps):
+    sols = _WORKER["sols"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for ns in sols:
+            ns.update()
+    return time.perf_counter() - t0, len(sols) * steps
+
+
+class CpuPort:
+    """The CPU oracle (NumPy restatement of the reference path) on ``cores`` spawned
+    processes, each owning a slice of the instances; solvers are built once."""
+
+    def __init__(self, specs, cores):
+        import multiprocessing as mp
+        self.chunks = [c for c in (specs[i::cores] for i in range(cores)) if c]
+        ctx = mp.get_context("spawn")
+        self.pools = []
+        # one BLAS thread per worker process: the processes are the parallelism
+        saved = {k: os.environ.get(k) for k in BLAS_ENV}
+        os.environ.update({k: "1" for k in BLAS_ENV})
+        try:
+            for c in self.chunks:
+                self.pools.append(ctx.Pool(1, initializer=_oracle_init, initargs=(c,)))
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    def step(self, steps=1):
+        """Advance every instance ``steps`` steps; returns (instance-steps done, wall s of stepping)."""
+        res = [p.apply_async(_oracle_steps, (steps,)) for p in self.pools]
+        out = [r.get() for r in res]
+        return sum(o[1] for o in out), max(o[0] for o in out)
+
+    def close(self):
+        for p in self.pools:
+            p.close()
+            p.join()
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/pgx_bench_clocks.csv"
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ GPU side
+def build_batch(specs):
+    from pypde_gb300.navier.fused import FusedBatch
+    from pypde_gb300.navier.rbc2d import NavierStokes
+    solvers = []
+    for shape, ra, dt, seed, amp, aspect in specs:
+        ns = NavierStokes(case="linear", shape=shape, ra=ra, pr=1.0, dt=dt, aspect=aspect, dealias=True,
+                          integrator="eu", beta=1.0, tsave=None)
+        ns.set_temperature_noise(seed, amp)
+        solvers.append(ns)
+    return solvers, FusedBatch(solvers)
+
+
+def time_steps(fn, steps, stream):
+    """Per-step CUDA events on ``stream``; returns the list of step times in ms."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def per_pass_times(fb, reps, stream):
+    import torch
+    out = []
+    for i in range(len(fb.launches)):
+        fb.run_pass(i)  # warm
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fb.run_pass(i)
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b) / reps)
+    return out
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    specs = workload_specs(args.workload, args.instances, rank)
+    cores = host_cores()
+
+    # CPU baseline first (spawned pool, before heavy GPU work), rank 0 only, N = 1 only
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sample = specs[::8] if args.workload == "c4" else specs
+        steps_cpu = 1 if args.workload == "c4" else (20 if args.workload == "c1" else 1)
+        ncores = min(cores, len(sample))
+        port = CpuPort(sample, ncores)
+        done, wall = port.step(steps_cpu)
+        port.close()
+        cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port",
+               "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (NumPy "
+                         "restatement of the reference path) in %d single-threaded processes, %.1f s of stepping"
+                         % (len(sample), len(specs), steps_cpu, ncores, wall)}
+
+    solvers, fb = build_batch(specs)
+    n_inst = len(solvers)
+    stream = torch.cuda.current_stream()
+    fb.capture(1)
+    state_bytes = fb.state_arena.numel() * 8
+    work_bytes = fb.scratch_bytes()
+
+    # warmup + timed region (graph replay), barrier + sync on both sides
+    for _ in range(args.warmup):
+        fb.step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    t0 = time.perf_counter()
+    step_ms = time_steps(fb.step, args.steps, stream)
+    wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = n_inst * world * args.steps / (total_ms / 1e3)
+    finite = int(sum(bool(torch.isfinite(I.arrays["TG"]).all()) for I in fb.insts))
+
+    # e2e: public API, state in pinned host memory, H2D before and D2H after every step
+    host = torch.empty(fb.state_arena.numel(), dtype=torch.float64, pin_memory=True)
+    host.copy_(fb.state_arena)
+
+    def e2e_step():
+        fb.state_arena.copy_(host, non_blocking=True)
+        fb.step()
+        host.copy_(fb.state_arena, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = time_steps(e2e_step, args.steps, stream)
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e = {"value": n_inst * world * args.steps / (e2e_total / 1e3), "unit": "instance-steps/s",
+           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}
+
+    if rank != 0:
+        return None
+
+    # roofline of the dominant pass: algorithmic flops / CUDA-event time per launch
+    pt = per_pass_times(fb, 5, stream)
+    work = fb.pass_work()
+    passes = []
+    for (name, fl, by), ms in zip(work, pt):
+        passes.append({"pass": name, "ms": round(ms, 4), "gflop": round(fl / 1e9, 4),
+                       "tflops": round(fl / (ms * 1e-3) / 1e12, 4), "frac_fp64": round(fl / (ms * 1e-3) / 1e12 /
+                                                                                         FP64_PEAK_TFLOPS, 4),
+                       "gb": round(by / 1e9, 5)})
+    dom = max(range(len(pt)), key=lambda i: pt[i])
+    fl_dom = work[dom][1]
+    achieved = fl_dom / (pt[dom] * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": "line_program_batched (%s)" % work[dom][0], "achieved": round(achieved, 4),
+                "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4),
+                "traffic": None,
+                "peak_source": "measured DFMA peak of this GB300 (profiles/gb300_fp64_probe.txt); the "
+                               "driver-written peak file carries only HBM and bf16",
+                "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2]}
+    step_fl = sum(w[1] for w in work)
+    step_fp64 = {"tflops": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12, 4),
+                 "frac": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12 / FP64_PEAK_TFLOPS, 4),
+                 "gflop_per_step": round(step_fl / 1e9, 3)}
+
+    # one by one on the per-instance GPU path (same fused kernels, one CUDA graph per instance)
+    plain = None
+    if n_inst > 1 and not args.no_plain:
+        per = []
+        for i in range(n_inst):
+            one = fb.single(i)
+            one.capture(1)
+            for _ in range(2):
+                one.step()
+            per.append(sum(time_steps(one.step, 3, stream)) / 3)
+            del one
+        plain = {"value": n_inst / (sum(per) / 1e3), "unit": "instance-steps/s",
+                 "how": "the same %d instances one at a time, per-instance CUDA graph of the fused step" % n_inst}
+    # op-by-op drop-in path (NavierStokes.update: one kernel per pypde operation) on a sample
+    eager = None
+    if not args.no_plain:
+        sample = solvers[: min(8, n_inst)]
+        for ns in sample:
+            ns.update()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for ns in sample:
+            for _ in range(2):
+                ns.update()
+        torch.cuda.synchronize()
+        dt_s = time.perf_counter() - t
+        eager = {"value": 2 * len(sample) / dt_s, "unit": "instance-steps/s",
+                 "how": "NavierStokes.update() op by op (plain drop-in path), %d instances x 2 steps, host "
+                        "wall clock" % len(sample)}
+
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "instance-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: seeded U(-1,1) temperature noise on the conductive profile (seeds 100+i)",
+        "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=n_inst), "instances_per_gpu": n_inst,
+                   "sizes": sorted({s[0] for s in specs}), "form": "batched, CUDA-graph replay of 10 fused passes",
+                   "l2": "no flush: the working set (state %.1f MB + scratch %.1f MB) exceeds the 129 MB L2"
+                         % (state_bytes / 1e6, work_bytes / 1e6), "parallelism": "instance-parallel"},
+        "e2e": e2e,
+        "gpu_launches": fb.launches_per_step * args.steps,
+        "roofline": roofline,
+        "step_fp64": step_fp64,
+        "passes": passes,
+        "plain": plain,
+        "eager": eager,
+        "finite_instances": finite,
+        "host_wall_s": round(wall, 3),
+    }
+    if clk:
+        line["clocks"] = clk
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU oracle (NumPy restatement of pypde's path; the reference
+    itself is Python and does not ship to the GPU host) on all host cores."""
+    if rank != 0:
+        return None
+    specs = workload_specs(args.workload, args.instances)
+    full = len(specs)
+    if args.workload == "c4":
+        specs = specs[::4]  # a bounded sample with the same size / Ra mix
+    cores = min(host_cores(), len(specs))
+    port = CpuPort(specs, cores)
+    for _ in range(max(args.warmup, 1)):
+        port.step(1)
+    total_done, total_wall = 0, 0.0
+    for _ in range(args.steps):
+        done, wall = port.step(1)
+        total_done += done
+        total_wall += wall
+    port.close()
+    value = total_done / total_wall
+    return {"metric": METRIC, "value": round(value, 3), "unit": "instance-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded U(-1,1) temperature noise (seeds 100+i)", "impl": "reference",
+            "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=full), "instances_per_gpu": full},
+            "cpu_baseline": {"value": round(value, 3), "unit": "instance-steps/s", "cores": cores, "kind": "port",
+                             "sample": "every %s instance (%d of %d, same size / Ra mix), 1 step per timed step, "
+                                       "%d single-threaded spawned processes running the CPU oracle (NumPy "
+                                       "restatement of the reference path)" % ("4th" if full != len(specs) else
+                                                                               "", len(specs), full, cores)},
+            "e2e": {"value": round(value, 3), "unit": "instance-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c4", choices=["c4", "c1", "c3"])
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+        line = run_gpu(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -406,7 +406,15 @@ def _dct_tables(n, fft):
 class _Instance:
     """Device state, scratch and operator tables of one RBC instance."""
 
-    def __init__(self, ns, fft):
+    STATE = ("UG", "VG", "TG", "PG", "PRES")
+
+    @staticmethod
+    def state_shapes(ns):
+        N, M = ns.shape
+        return {"UG": (N - 2, M - 2), "VG": (N - 2, M - 2), "TG": (N - 2, M - 2), "PG": (N - 2, M - 2),
+                "PRES": (N, M)}
+
+    def __init__(self, ns, fft, views=None):
         if ns.nstage != 1 or ns.beta != 1.0:
             raise NotImplementedError("the fused step covers IMEX Euler with beta = 1; use update() otherwise")
         self.ns = ns
@@ -418,7 +426,11 @@ class _Instance:
         a = {}
         # state (shared with the NavierStokes object's fields)
         for key, fld in (("UG", ns.U), ("VG", ns.V), ("TG", ns.T), ("PG", ns.P), ("PRES", ns.pres)):
-            fld.vhat = a[key] = fld.vhat.contiguous()
+            if views is not None:
+                views[key].copy_(fld.vhat)
+                fld.vhat = a[key] = views[key]
+            else:
+                fld.vhat = a[key] = fld.vhat.contiguous()
         a["TBCC"] = ns.Tbc_cheby.contiguous()
         a["DTB1"] = ns.dTbcdz1.contiguous()
         a["DTB2"] = ns.dTbcdz2.contiguous()
@@ -519,7 +531,18 @@ class FusedBatch:
             raise ValueError("all instances of a batch need the same temperature basis")
         sizes = [(int(1.5 * ns.shape[0]), int(1.5 * ns.shape[1])) if ns.dealias else ns.shape for ns in self.solvers]
         self.fft = all(fft_ok(n) for s in sizes for n in s)
-        self.insts = [_Instance(ns, self.fft) for ns in self.solvers]
+        # all instance states live in one arena: one H2D / D2H copy moves the whole batch
+        shapes = [_Instance.state_shapes(ns) for ns in self.solvers]
+        total = sum(r * c for sh in shapes for (r, c) in sh.values())
+        self.state_arena = torch.zeros(total, dtype=DTYPE, device=device())
+        self.insts, off = [], 0
+        for ns, sh in zip(self.solvers, shapes):
+            views = {}
+            for key in _Instance.STATE:
+                r, c = sh[key]
+                views[key] = self.state_arena[off:off + r * c].view(r, c)
+                off += r * c
+            self.insts.append(_Instance(ns, self.fft, views))
         self.progs = build_programs(tkinds.pop(), self.fft)
         self._build_launches()
         self.graph = None
@@ -592,6 +615,92 @@ class FusedBatch:
     @property
     def launches_per_step(self):
         return len(self.launches)
+
+    def single(self, i):
+        """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""
+        one = FusedBatch.__new__(FusedBatch)
+        one.solvers, one.insts, one.fft, one.progs = [self.solvers[i]], [self.insts[i]], self.fft, self.progs
+        one.state_arena = None
+        one._build_launches()
+        one.graph = None
+        return one
+
+    def scratch_bytes(self):
+        return sum(t.numel() * 8 for I in self.insts for k, t in I.arrays.items())
+
+    def pass_work(self):
+        """Algorithmic FP64 flops and HBM bytes per launch of every pass (all instances)."""
+        out = []
+        for prog in self.progs:
+            fl = by = 0.0
+            for I in self.insts:
+                f, b = program_work(prog, I)
+                fl += f
+                by += b
+            out.append((prog.name, fl, by))
+        return out
+
+
+def _log2(x):
+    return float(np.log2(x))
+
+
+def program_work(prog, I):
+    """Algorithmic work of ``prog`` on instance ``I``: (flops, bytes).
+
+    Counts per line of n elements: DCT-I 2.5 n log2(2(n-1)) (the FFT count);
+    stencil / transpose 2 per output; derivative 2 per element and pass;
+    offset-2 TDMA 5; four-diagonal sweep 7; Poisson sweep 9; banded 2 per
+    diagonal and row; dense 2 per column and row; scale / mul 1, axpy /
+    load-add 2.  Bytes: 8 per element loaded or stored.
+    """
+    lines = I.lens[prog.lines]
+    slen = [0] * 8
+    fl = by = 0.0
+    for o in prog.ops:
+        code = o.code
+        if code == _lib.OP["LOAD"]:
+            slen[o.a] = I.lens[o.len]
+            by += 8.0 * I.lens[o.len] * lines
+            if o.par >= 0 or o.alpha != 1.0:
+                fl += slen[o.a] * lines
+        elif code in (_lib.OP["LOAD_ADD"], _lib.OP["LOAD_MUL"]):
+            by += 8.0 * slen[o.a] * lines
+            fl += 2.0 * slen[o.a] * lines
+        elif code in (_lib.OP["STORE"], _lib.OP["STORE_ADD"]):
+            by += 8.0 * slen[o.a] * lines
+        elif code == _lib.OP["SCALE"]:
+            fl += slen[o.a] * lines
+        elif code in (_lib.OP["AXPY"], _lib.OP["MUL"], _lib.OP["COPY"]):
+            slen[o.a] = slen[o.b] if code == _lib.OP["COPY"] else max(slen[o.a], slen[o.b])
+            fl += (2.0 if code == _lib.OP["AXPY"] else (1.0 if code == _lib.OP["MUL"] else 0.0)) * slen[o.a] * lines
+        elif code == _lib.OP["SETLEN"]:
+            slen[o.a] = I.lens[o.len]
+        elif code == _lib.OP["STENCIL"]:
+            slen[o.a] += 2
+            fl += 2.0 * slen[o.a] * lines
+        elif code == _lib.OP["STENCIL_T"]:
+            slen[o.a] -= 2
+            fl += 2.0 * slen[o.a] * lines
+        elif code == _lib.OP["TDMA2"]:
+            fl += 5.0 * slen[o.a] * lines
+        elif code == _lib.OP["DIFF"]:
+            fl += 2.0 * o.k * slen[o.a] * lines
+        elif code == _lib.OP["DCT"]:
+            n = slen[o.a]
+            fl += 2.5 * n * _log2(2 * (n - 1)) * lines
+        elif code == _lib.OP["BANDED"]:
+            slen[o.a] = I.lens[o.len]
+            fl += 2.0 * o.k * slen[o.a] * lines
+        elif code == _lib.OP["DENSE"]:
+            cols = slen[o.a]
+            slen[o.a] = I.lens[o.len]
+            fl += 2.0 * cols * slen[o.a] * lines
+        elif code == _lib.OP["FDMA"]:
+            fl += 7.0 * slen[o.a] * lines
+        elif code == _lib.OP["POISSON"]:
+            fl += 9.0 * slen[o.a] * lines
+    return fl, by
 
 
 class FusedStep(FusedBatch):
