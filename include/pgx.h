@@ -80,18 +80,20 @@ enum pgx_opcode {
   PGX_OP_SETLEN = 10,   /* zero-pad / truncate slot a to len                 */
   PGX_OP_STENCIL = 11,  /* slot a (M) = S slot a (M+2); mat: S[i+2,i]        */
   PGX_OP_STENCIL_T = 12,/* slot a (N) = S^T slot a (N-2); mat: S[i+2,i]      */
-  PGX_OP_TDMA2 = 13,    /* slot a = (S^T S)^-1 slot a; mat: (a,rden,w) per i */
-  PGX_OP_DIFF = 14,     /* slot a = D^k slot a (Chebyshev recurrence)        */
+  PGX_OP_TDMA2 = 13,    /* slots a..a+b-1 = (S^T S)^-1 slot; mat: (a,rden,w) per i */
+  PGX_OP_DIFF = 14,     /* slots a..a+b-1 = D^k slot (Chebyshev recurrence)  */
   PGX_OP_DCT = 15,      /* slot a = DCT-I slot a; k = mode; mat: twiddles    */
   PGX_OP_BANDED = 17,   /* slot a = A slot a; k diagonals from offset b step 2, rows len; mat [k][rows] */
   PGX_OP_DENSE = 18,    /* slot a = A slot a; A is len x slen row-major       */
-  PGX_OP_FDMA = 19,     /* in-place -2/0/+2/+4 LU solve; mat: [l|dinv|u1|u2]  */
+  PGX_OP_FDMA = 19,     /* in-place -2/0/+2/+4 LU solve of slots a..a+b-1, table mat+s: [l|dinv|u1|u2] */
   PGX_OP_POISSON = 20,  /* like FDMA with per-line factors (line j at j*4*n)  */
   PGX_OP_ZERO00 = 21    /* element 0 of the instance's line 0 = 0            */
 };
 
 enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2 };
 
+/* Chain ops (DIFF, TDMA2, FDMA) act on the b consecutive slots a..a+b-1 at
+ * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset. */
 typedef struct pgx_op {
   int16_t code, a, b, arr, mat, len, par, k;
   double alpha;                    /* scalar; multiplied by par[par] when par >= 0 */

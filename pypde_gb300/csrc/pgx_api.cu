@@ -71,6 +71,9 @@ static int check_program(const pgx_program* P) {
     if (op.a < 0 || op.a >= P->nslots) return PGX_E_ARG;
     const bool uses_b = op.code == PGX_OP_AXPY || op.code == PGX_OP_MUL || op.code == PGX_OP_COPY;
     if (uses_b && (op.b < 0 || op.b >= P->nslots)) return PGX_E_ARG;
+    const bool chain = op.code == PGX_OP_DIFF || op.code == PGX_OP_TDMA2 || op.code == PGX_OP_FDMA;
+    if (chain && op.a + (op.b > 1 ? op.b : 1) > P->nslots) return PGX_E_ARG;
+    if (chain && op.code == PGX_OP_FDMA && op.mat + (op.b > 1 ? op.b : 1) > PGX_MAX_MAT) return PGX_E_ARG;
     if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;
   }
   int64_t need = pgx_program_smem(P) + 1024;

@@ -219,24 +219,34 @@ __device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 }
 
 // ------------------------------------------------ sequential parity chains
-// Thread (t, p) owns the chain of line t with indices = p (mod 2).
-__device__ __forceinline__ bool chain_of(const Ctx& c, int& t, int& p) {
-  if (c.tid >= 2 * c.tb) return false;
-  p = c.tid / c.tb;
-  t = c.tid - p * c.tb;
+// A chain op sweeps `ns` consecutive slots a, a+1, ... at once (independent
+// solves of one pass run concurrently, so every warp has chains to run).
+// Thread (s, p, t) owns the chain of line t of slot a+s with indices = p (mod 2).
+__device__ __forceinline__ bool chain_of(const Ctx& c, int ns, int& s, int& t, int& p) {
+  if (c.tid >= 2 * c.tb * ns) return false;
+  s = c.tid / (2 * c.tb);
+  int r = c.tid - s * 2 * c.tb;
+  p = r / c.tb;
+  t = r - p * c.tb;
   return true;
 }
+__device__ __forceinline__ int nslot_of(const pgx_op& op) { return op.b > 1 ? op.b : 1; }
 
 // (S^T S) x = d with the offset-2 TDMA; table interleaved per index i as
 // (aa_i, rden_i, w_i), so one long table serves every system length n:
 //   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}.
 // The last two w_i of a chain multiply x_{n}, x_{n+1} = 0 and are never used.
 __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
-  int t, p;
-  const int n = c.slen[op.a];
-  if (chain_of(c, t, p) && p < n) {
+  int s, t, p;
+  const int ns = nslot_of(op);
+  for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
+    Ctx cc = c;
+    cc.tid = c.tid + base;
+    if (!chain_of(cc, ns, s, t, p)) continue;
+    const int n = c.slen[op.a + s];
+    if (p >= n) continue;
     const double* tab = I.mat[op.mat];
-    double* x = slot_ptr(c, op.a) + t * c.lcap;
+    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
     double g = 0.0;
     int i = p;
     for (; i < n; i += 2) {
@@ -251,28 +261,30 @@ __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
 }
 
-// One Chebyshev derivative (differentiate_cheby.f90:28-53):
+// Chebyshev derivative in place (differentiate_cheby.f90:28-53), one thread per
+// (slot, line), both parity chains interleaved:
 //   dc_{n-1} = 0, dc_j = dc_{j+2} + 2(j+1) c_{j+1} (j = n-2..1), dc_0 = dc_2/2 + c_1.
-__device__ void op_diff_once(Ctx& c, int slot) {
-  const int n = c.slen[slot];
-  const double* x = slot_ptr(c, slot);
-  double* y = spare_ptr(c);
-  zero_tail(c, y, n - 1);
-  int t, p;
-  if (chain_of(c, t, p)) {
-    const double* xl = x + t * c.lcap;
-    double* yl = y + t * c.lcap;
-    int j = n - 2;
-    if ((j & 1) != p) --j;
-    double acc = 0.0;
-    for (; j >= 1; j -= 2) {
-      acc = fma(c_twok.v[j + 1], xl[j + 1], acc);
-      yl[j] = acc;
+// c_{j+1} is kept in a register before its slot entry is overwritten.
+__device__ void op_diff(Ctx& c, const pgx_op& op) {
+  const int ns = nslot_of(op);
+  for (int w = c.tid; w < ns * c.tb; w += c.nthreads) {
+    const int s = w / c.tb, t = w - s * c.tb;
+    const int n = c.slen[op.a + s];
+    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    for (int rep = 0; rep < op.k; ++rep) {
+      double acc[2] = {0.0, 0.0};
+      double cnext = x[n - 1];  // c_{j+1}
+      x[n - 1] = 0.0;
+      for (int j = n - 2; j >= 1; --j) {
+        const double cj = x[j];
+        const double v = fma(c_twok.v[j + 1], cnext, acc[j & 1]);
+        acc[j & 1] = v;
+        x[j] = v;
+        cnext = cj;
+      }
+      x[0] = fma(0.5, acc[0], cnext);  // dc_2 / 2 + c_1
     }
-    if (p == 0) yl[0] = fma(0.5, (n > 2 ? yl[2] : 0.0), xl[1]);
   }
-  __syncthreads();
-  swap_spare(c, slot);
 }
 
 // In-place banded LU sweep for offsets -2, 0, +2, +4 (fdma.f90:1-38) with
@@ -299,16 +311,21 @@ __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, 
   }
 }
 
+// FDMA over ns slots: slot a+s uses factor table mat+s.  POISSON (per_line):
+// single table with per-line factors.
 __device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line) {
-  int t, p;
-  const int n = c.slen[op.a];
-  if (chain_of(c, t, p) && p < n) {
+  int s, t, p;
+  const int ns = nslot_of(op);
+  for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
+    Ctx cc = c;
+    cc.tid = c.tid + base;
+    if (!chain_of(cc, ns, s, t, p)) continue;
+    const int n = c.slen[op.a + s];
     const int line = c.l0 + t;
-    if (line < c.nlines) {
-      const double* tab = I.mat[op.mat];
-      if (per_line) tab += (size_t)line * 4 * n;
-      fdma_chain(slot_ptr(c, op.a) + t * c.lcap, tab, n, p);
-    }
+    if (p >= n || line >= c.nlines) continue;
+    const double* tab = I.mat[op.mat + (per_line ? 0 : s)];
+    if (per_line) tab += (size_t)line * 4 * n;
+    fdma_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
   }
 }
 
@@ -374,48 +391,102 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
-template <int R>
+// One radix-R Stockham stage over `npairs` pairs of lines.
+//   FIRST: the input is the even extension of slot lines (2p, 2p+1), read straight
+//          from the slot with the backward pre-scale folded in (no copy pass);
+//   LAST:  outputs k <= N are written straight back to the slot lines with the
+//          forward post-scale (no extraction pass).
+template <int R, bool FIRST, bool LAST>
 __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src, double2* dst, const double2* tw,
-                                               int L, int Ns, int npairs) {
+                                               int L, int Ns, int npairs, double* x, int mode) {
   const int LR = L / R;
   const int step = L / (Ns * R);
+  const int N = L >> 1;
+  const double invN = 1.0 / N;
   for (int idx = c.tid; idx < npairs * LR; idx += c.nthreads) {
     int pr = idx / LR, j = idx - pr * LR;
-    const double2* s = src + pr * c.fft_stride;
-    double2* d = dst + pr * c.fft_stride;
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
     int k = j % Ns;
     double2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = s[j + r * LR];
+    for (int r = 0; r < R; ++r) {
+      const int m = j + r * LR;
+      if (FIRST) {
+        const int sidx = m <= N ? m : L - m;
+        double a = x[t0 * c.lcap + sidx];
+        double b = two ? x[(t0 + 1) * c.lcap + sidx] : 0.0;
+        if (mode == PGX_DCT_BWD) {
+          // g_s = (-1)^s c_s, doubled at both ends, times the final 1/2
+          double w = (sidx == 0 || sidx == N) ? 1.0 : 0.5;
+          if (sidx & 1) w = -w;
+          a *= w;
+          b *= w;
+        }
+        v[r] = make_double2(a, b);
+      } else {
+        v[r] = src[pr * c.fft_stride + m];
+      }
+    }
     if (k != 0) {
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + k * r * step));
     }
-    int base = (j - k) * R + k;
+    double2 o[R];
     if (R == 2) {
-      d[base] = cadd(v[0], v[1]);
-      d[base + Ns] = csub(v[0], v[1]);
+      o[0] = cadd(v[0], v[1]);
+      o[1] = csub(v[0], v[1]);
     } else if (R == 4) {
       double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
       double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
-      d[base] = cadd(a, e);
-      d[base + 2 * Ns] = csub(a, e);
-      // -i*f = (f.y, -f.x)
-      d[base + Ns] = make_double2(b.x + f.y, b.y - f.x);
-      d[base + 3 * Ns] = make_double2(b.x - f.y, b.y + f.x);
+      o[0] = cadd(a, e);
+      o[2] = csub(a, e);
+      o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
+      o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
     } else {  // R == 3, W3 = -1/2 - i sqrt(3)/2
       const double h = 0.86602540378443864676;
       double2 t1 = cadd(v[1], v[2]);
       double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
       double2 t3 = csub(v[1], v[2]);
-      d[base] = cadd(v[0], t1);
-      // out1 = t2 - i h t3 ; out2 = t2 + i h t3
-      d[base + Ns] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));
-      d[base + 2 * Ns] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));
+      o[0] = cadd(v[0], t1);
+      o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));  // t2 - i h t3
+      o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));  // t2 + i h t3
+    }
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int kk = base + q * Ns;
+      if (LAST) {
+        if (kk <= N) {
+          double2 z = o[q];
+          if (mode == PGX_DCT_FWD) {
+            // c_k = m_k (-1)^k y_k / (2N)
+            double sc = (kk == 0 || kk == N) ? 0.5 * invN : invN;
+            if (kk & 1) sc = -sc;
+            z.x *= sc;
+            z.y *= sc;
+          }
+          x[t0 * c.lcap + kk] = z.x;
+          if (two) x[(t0 + 1) * c.lcap + kk] = z.y;
+        }
+      } else {
+        dst[pr * c.fft_stride + kk] = o[q];
+      }
     }
   }
 }
 
+__device__ __forceinline__ int next_radix(int rem) { return (rem & 3) == 0 ? 4 : ((rem & 1) == 0 ? 2 : 3); }
+
+template <bool FIRST, bool LAST>
+__device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double2* src, double2* dst, const double2* tw,
+                                               int L, int Ns, int npairs, double* x, int mode) {
+  if (R == 4) stockham_stage<4, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
+  else if (R == 2) stockham_stage<2, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
+  else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
+}
+
+// DCT-I of the slot (length n) in place, see stockham_stage for the data path.
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
   const int N = n - 1, L = 2 * N;
@@ -423,53 +494,47 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, op.a);
   const int npairs = (c.tb + 1) >> 1;
-  // backward pre-scale: g_k = (-1)^k c_k, doubled at both ends, times the final 1/2
-  if (mode == PGX_DCT_BWD) {
+  int nst = 0;
+  for (int rem = L; rem > 1; rem /= next_radix(rem)) ++nst;
+  double2* bufs[2] = {c.f0, c.f1};
+  int Ns = 1, rem = L, cur = 0;
+  for (int s = 0; s < nst; ++s) {
+    const int R = next_radix(rem);
+    const double2* src = bufs[cur];
+    double2* dst = bufs[cur ^ 1];
+    if (s == 0) {
+      if (nst == 1) {
+        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, mode);
+      } else {
+        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, mode);
+        cur = 0;
+        Ns *= R;
+        rem /= R;
+        __syncthreads();
+        continue;
+      }
+    } else if (s == nst - 1) {
+      stage_dispatch<false, true>(R, c, src, nullptr, tw, L, Ns, npairs, x, mode);
+    } else {
+      stage_dispatch<false, false>(R, c, src, dst, tw, L, Ns, npairs, x, mode);
+      cur ^= 1;
+    }
+    Ns *= R;
+    rem /= R;
+    __syncthreads();
+  }
+  if (nst == 1) {  // tiny transform: copy the single stage's output back
+    const double invN = 1.0 / N;
     for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
       int t = idx / n, k = idx - t * n;
-      double s = (k == 0 || k == N) ? 1.0 : 0.5;
-      x[t * c.lcap + k] *= (k & 1) ? -s : s;
+      double2 z = c.f0[(t >> 1) * c.fft_stride + k];
+      double y = (t & 1) ? z.y : z.x;
+      if (mode == PGX_DCT_FWD) {
+        double sc = (k == 0 || k == N) ? 0.5 * invN : invN;
+        y *= (k & 1) ? -sc : sc;
+      }
+      x[t * c.lcap + k] = y;
     }
-    __syncthreads();
-  }
-  // even extension of lines (2p, 2p+1) into z
-  for (int idx = c.tid; idx < npairs * L; idx += c.nthreads) {
-    int pr = idx / L, m = idx - pr * L;
-    int s = m <= N ? m : L - m;
-    int t0 = 2 * pr, t1 = t0 + 1;
-    double a = x[t0 * c.lcap + s];
-    double b = t1 < c.tb ? x[t1 * c.lcap + s] : 0.0;
-    c.f0[pr * c.fft_stride + m] = make_double2(a, b);
-  }
-  __syncthreads();
-  double2* src = c.f0;
-  double2* dst = c.f1;
-  int Ns = 1, rem = L;
-  while (rem > 1) {
-    if ((rem & 3) == 0) {
-      stockham_stage<4>(c, src, dst, tw, L, Ns, npairs);
-      Ns *= 4; rem >>= 2;
-    } else if ((rem & 1) == 0) {
-      stockham_stage<2>(c, src, dst, tw, L, Ns, npairs);
-      Ns *= 2; rem >>= 1;
-    } else {
-      stockham_stage<3>(c, src, dst, tw, L, Ns, npairs);
-      Ns *= 3; rem /= 3;
-    }
-    __syncthreads();
-    double2* tmp = src; src = dst; dst = tmp;
-  }
-  // output k = 0..N; forward post-scale: c_k = m_k (-1)^k y_k / (2N)
-  const double inv = (mode == PGX_DCT_FWD) ? 1.0 / N : 1.0;
-  for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
-    int t = idx / n, k = idx - t * n;
-    double2 z = src[(t >> 1) * c.fft_stride + k];
-    double y = (t & 1) ? z.y : z.x;
-    if (mode == PGX_DCT_FWD) {
-      double s = (k == 0 || k == N) ? 0.5 * inv : inv;
-      y *= (k & 1) ? -s : s;
-    }
-    x[t * c.lcap + k] = y;
   }
 }
 
@@ -514,9 +579,7 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
       case PGX_OP_STENCIL: op_stencil(c, op, I); break;
       case PGX_OP_STENCIL_T: op_stencil_t(c, op, I); break;
       case PGX_OP_TDMA2: op_tdma2(c, op, I); break;
-      case PGX_OP_DIFF:
-        for (int r = 0; r < op.k; ++r) op_diff_once(c, op.a);
-        break;
+      case PGX_OP_DIFF: op_diff(c, op); break;
       case PGX_OP_DCT: op_dct(c, op, I); break;
       case PGX_OP_BANDED: op_banded(c, op, I); break;
       case PGX_OP_DENSE: op_dense(c, op, I); break;

@@ -119,12 +119,24 @@ class Prog:
     def dense(self, s, name, rows):
         self.add("DENSE", s, mat=name, len=rows)
 
-    def fdma(self, s, name):
-        self.add("FDMA", s, mat=name)
+    def fdma(self, s, names):
+        """One FDMA op over consecutive slots s, s+1, ... with factor tables ``names``."""
+        if isinstance(names, str):
+            names = [names]
+        first = None
+        for i, nm in enumerate(names):
+            key = "%s#%d.%d" % (nm, len(self.ops), i)  # fresh keys -> consecutive table indices
+            idx = self._m(key)
+            first = idx if first is None else first
+            assert idx == first + i
+        self.ops.append(_lib.op("FDMA", a=s, b=len(names), mat=first))
+
+    def tdma_multi(self, s, count, kind):
+        self.add("TDMA2", s, b=count, mat="tdma_" + kind)
 
 
 def build_programs(tkind, fft):
-    """The ten passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
+    """The eleven passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
     ("CD" for the linear / zero cases, "CN" for rbc)."""
     P = []
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
@@ -182,8 +194,8 @@ def build_programs(tkind, fft):
     p.store(2, "TSY")
     P.append(p)
 
-    # P3 (x, lines M): forward x-transform, right-hand sides, B_x, ADI x-sweep
-    p = Prog("P3", 0, L_M, 3)
+    # P3 (x, lines M): forward x-transform and right-hand sides
+    p = Prog("P3", 0, L_M, 2)
     for F in "UVT":
         p.load(0, "C_" + F, L_ND)
         p.dct(0, FWD, fft)
@@ -201,33 +213,41 @@ def build_programs(tkind, fft):
             p.axpy(0, 1, par=P_DT)
         else:
             p.load_add(0, "DTB2", par=P_DTK)
-        p.banded(0, "Bx", 0, 3, L_NG)
-        p.fdma(0, "Ax_T" if F == "T" else "Ax_U")
-        p.store(0, "Q1_" + F)
-        p.load(2, F + "G", L_NG)
-        p.banded(2, "BSx_T" if F == "T" else "BSx_U", -2, 4, L_NG)
-        p.fdma(2, "Ax_T" if F == "T" else "Ax_U")
-        p.store(2, "Q2_" + F)
+        p.store(0, "RHS_" + F)
+    P.append(p)
+
+    # P3s (x, lines M): B_x, ADI x-sweep of the rhs and of the old-time terms B_x S_x F;
+    # the six independent sweeps run as one multi-slot chain op
+    p = Prog("P3s", 0, L_M, 6)
+    ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
+    for i, F in enumerate("UVT"):
+        p.load(i, "RHS_" + F, L_N)
+        p.banded(i, "Bx", 0, 3, L_NG)
+        p.load(3 + i, F + "G", L_NG)
+        p.banded(3 + i, "BSx_T" if F == "T" else "BSx_U", -2, 4, L_NG)
+    p.fdma(0, [ax[F] for F in "UVT"] + [ax[F] for F in "UVT"])
+    for i, F in enumerate("UVT"):
+        p.store(i, "Q1_" + F)
+        p.store(3 + i, "Q2_" + F)
     P.append(p)
 
     # P4 (y, lines N-2): B_y, ADI y-sweep -> U*, V*, T; divergence pieces
-    p = Prog("P4", 1, L_NG, 3)
-    for F in "UVT":
-        p.load(0, "Q1_" + F, L_M)
-        p.banded(0, "By", 0, 3, L_MG)
-        p.load(1, "Q2_" + F, L_MG)
-        p.banded(1, "BSy", -2, 4, L_MG)
-        p.axpy(0, 1)
-        p.fdma(0, "Ay_T" if F == "T" else "Ay_U")
-        p.store(0, F + "G")
-        if F == "U":
-            p.stencil(0, "CD")
-            p.store(0, "W1")
-        elif F == "V":
-            p.stencil(0, "CD")
-            p.diff(0)
-            p.scale(0, par=P_ISZ)
-            p.store(0, "W2")
+    p = Prog("P4", 1, L_NG, 4)
+    for i, F in enumerate("UVT"):
+        p.load(i, "Q1_" + F, L_M)
+        p.banded(i, "By", 0, 3, L_MG)
+        p.load(3, "Q2_" + F, L_MG)
+        p.banded(3, "BSy", -2, 4, L_MG)
+        p.axpy(i, 3)
+    p.fdma(0, ["Ay_U", "Ay_U", "Ay_T"])
+    for i, F in enumerate("UVT"):
+        p.store(i, F + "G")
+    p.stencil(0, "CD")
+    p.store(0, "W1")
+    p.stencil(1, "CD")
+    p.diff(1)
+    p.scale(1, par=P_ISZ)
+    p.store(1, "W2")
     P.append(p)
 
     # P5 (x, lines M): divergence, pres -= nu div, B_x div
@@ -274,33 +294,34 @@ def build_programs(tkind, fft):
     P.append(p)
 
     # P9 (x, lines M): pres += S_x S_y P / dt; grad P -> from_chebyshev along x
-    p = Prog("P9", 0, L_M, 2)
+    p = Prog("P9", 0, L_M, 3)
     p.load(0, "Y1", L_NG)
     p.stencil(0, "CN")
-    p.load(1, "PRES", L_N)
-    p.axpy(1, 0, par=P_IDT)
-    p.store(1, "PRES")
+    p.load(2, "PRES", L_N)
+    p.axpy(2, 0, par=P_IDT)
+    p.store(2, "PRES")
     p.diff(0)
     p.scale(0, par=P_ISX)
     p.stencil_t(0, "CD")
-    p.tdma(0, "CD")
-    p.store(0, "G1")
     p.load(1, "Y2", L_NG)
     p.stencil(1, "CN")
     p.stencil_t(1, "CD")
-    p.tdma(1, "CD")
+    p.tdma_multi(0, 2, "CD")
+    p.store(0, "G1")
     p.store(1, "G2")
     P.append(p)
 
     # P10 (y, lines N-2): from_chebyshev along y, velocity correction
-    p = Prog("P10", 1, L_NG, 2)
-    for F, G in (("U", "G1"), ("V", "G2")):
-        p.load(0, G, L_M)
-        p.stencil_t(0, "CD")
-        p.tdma(0, "CD")
-        p.load(1, F + "G", L_MG)
-        p.axpy(1, 0, alpha=-1.0)
-        p.store(1, F + "G")
+    p = Prog("P10", 1, L_NG, 3)
+    p.load(0, "G1", L_M)
+    p.stencil_t(0, "CD")
+    p.load(1, "G2", L_M)
+    p.stencil_t(1, "CD")
+    p.tdma_multi(0, 2, "CD")
+    for i, F in enumerate("UV"):
+        p.load(2, F + "G", L_MG)
+        p.axpy(2, i, alpha=-1.0)
+        p.store(2, F + "G")
     P.append(p)
     return P
 
@@ -438,6 +459,7 @@ class _Instance:
             a["A_" + F + "0"] = z(Nd, M - 2)
             a["A_" + F + "x"] = z(Nd, M - 2)
             a["C_" + F] = z(Nd, M)
+            a["RHS_" + F] = z(N, M)
             a["Q1_" + F] = z(N - 2, M)
             a["Q2_" + F] = z(N - 2, M - 2)
         a["DPZ"] = z(N, M)
@@ -496,7 +518,8 @@ class _Instance:
             A.ptr, A.s0, A.s1, A.n0, A.n1 = t.data_ptr(), t.stride(0), t.stride(1), t.shape[0], t.shape[1]
         dct = self.dct_x if prog.axis == 0 else self.dct_y
         for name, idx in prog.mats.items():
-            v = dct[name] if name.startswith("dct") else self.tables[name]
+            base = name.split("#")[0]
+            v = dct[base] if base.startswith("dct") else self.tables[base]
             inst.mat[idx] = v if isinstance(v, int) else v.data_ptr()
         for i, n in enumerate(self.lens):
             inst.len[i] = n
@@ -505,20 +528,66 @@ class _Instance:
             inst.par[i] = v
 
 
-def _pick(lines_total, lcap, nbuf, fft_n, max_lines):
-    """Lines per CTA and threads for a pass over ``lines_total`` lines (all instances)."""
+def program_maxlen(prog, lens):
+    """Longest line a slot of ``prog`` holds for an instance with lengths ``lens``."""
+    slen = [0] * 8
+    m = 0
+    for o in prog.ops:
+        c = o.code
+        if c in (_lib.OP["LOAD"], _lib.OP["SETLEN"], _lib.OP["BANDED"], _lib.OP["DENSE"]):
+            slen[o.a] = lens[o.len]
+        elif c == _lib.OP["STENCIL"]:
+            slen[o.a] += 2
+        elif c == _lib.OP["STENCIL_T"]:
+            slen[o.a] -= 2
+        elif c in (_lib.OP["AXPY"], _lib.OP["MUL"]):
+            slen[o.a] = max(slen[o.a], slen[o.b])
+        elif c == _lib.OP["COPY"]:
+            slen[o.a] = slen[o.b]
+        m = max(m, slen[o.a])
+    return m
+
+
+CHAIN_OPS = ("FDMA", "POISSON", "TDMA2")
+SMEM_PER_SM = 227 * 1024
+
+
+def _pick(prog, lines_total, lcap, fft_n, max_lines):
+    """Lines per CTA and threads for one pass over ``lines_total`` lines (all instances).
+
+    FFT passes: at most ~113 KB of shared memory per CTA so two CTAs share an SM
+    (one computes while the other waits at a barrier).  Passes dominated by
+    sequential banded sweeps: many lines per CTA, because each (line, parity)
+    chain is one thread and the FP64 pipe of every SM sub-partition needs a
+    warp of chains.
+    """
+    nbuf = prog.nslots + 1
     per_line = 8 * nbuf * lcap + (32 * (fft_n - 1) if fft_n > 1 else 0)
-    budget = 200 * 1024 - 1024
-    tbmax = max(1, budget // per_line)
-    tb = max(1, -(-lines_total // (2 * 152)))
+    chains = any(o.code in [_lib.OP[k] for k in CHAIN_OPS] for o in prog.ops)
     if fft_n > 1:
-        tb = max(tb, 2)
-    tb = min(tb, tbmax, 32, max(max_lines, 1))
-    if fft_n > 1 and tb > 1 and tb % 2:
-        tb -= 1
-    work = tb * lcap
-    nt = min(512, max(64, 32 * -(-work // (32 * 2))))
-    return tb, nt
+        budget = SMEM_PER_SM // 2 - 2048
+        cap = 16
+    elif chains:
+        budget = SMEM_PER_SM - 4096
+        cap = 64
+    else:
+        budget = SMEM_PER_SM // 2 - 2048
+        cap = 32
+    tbmax = max(1, budget // per_line)
+    want = max(1, -(-lines_total // (2 * 152)))  # at least two CTAs per SM when there is work
+    tb = max(1, min(cap, tbmax, want, max(max_lines, 1)))
+    if fft_n > 1:
+        tb = min(max(tb, 2), max(2, tbmax - tbmax % 2))
+        tb -= tb % 2
+    # one thread per (slot, line, parity) chain of the widest chain op
+    width = 1
+    for o in prog.ops:
+        if o.code in (_lib.OP["FDMA"], _lib.OP["TDMA2"], _lib.OP["POISSON"]):
+            width = max(width, 2 * max(o.b, 1))
+        elif o.code == _lib.OP["DIFF"]:
+            width = max(width, max(o.b, 1))
+    nt = max(256, 32 * -(-width * tb // 32))
+    return tb, min(nt, 1024)
 
 
 class FusedBatch:
@@ -552,14 +621,10 @@ class FusedBatch:
         self.launches = []
         for prog in self.progs:
             lines = [I.lines(prog) for I in self.insts]
-            maxlen = 0
-            for I in self.insts:
-                lens = I.lens
-                m = max(lens[L_ND], lens[L_N]) if prog.axis == 0 else max(lens[L_MD], lens[L_M])
-                maxlen = max(maxlen, m)
+            maxlen = max(program_maxlen(prog, I.lens) for I in self.insts)
             lcap = (maxlen + 1) | 1
-            fft_n = maxlen if (prog.has_dct and self.fft) else 0
-            tb, nt = _pick(sum(lines), lcap, prog.nslots + 1, fft_n, max(lines))
+            fft_n = max(I.lens[L_ND + prog.axis] for I in self.insts) if (prog.has_dct and self.fft) else 0
+            tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
             P = _lib.PgxProgram()
             P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
             P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
@@ -683,9 +748,9 @@ def program_work(prog, I):
             slen[o.a] -= 2
             fl += 2.0 * slen[o.a] * lines
         elif code == _lib.OP["TDMA2"]:
-            fl += 5.0 * slen[o.a] * lines
+            fl += 5.0 * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
         elif code == _lib.OP["DIFF"]:
-            fl += 2.0 * o.k * slen[o.a] * lines
+            fl += 2.0 * o.k * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
         elif code == _lib.OP["DCT"]:
             n = slen[o.a]
             fl += 2.5 * n * _log2(2 * (n - 1)) * lines
@@ -697,7 +762,7 @@ def program_work(prog, I):
             slen[o.a] = I.lens[o.len]
             fl += 2.0 * cols * slen[o.a] * lines
         elif code == _lib.OP["FDMA"]:
-            fl += 7.0 * slen[o.a] * lines
+            fl += 7.0 * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
         elif code == _lib.OP["POISSON"]:
             fl += 9.0 * slen[o.a] * lines
     return fl, by

@@ -68,17 +68,22 @@ def test_fused_programs_fit_the_abi(tkind, fft):
     from pypde_gb300 import _lib
     from pypde_gb300.navier.fused import build_programs
     progs = build_programs(tkind, fft)
-    assert len(progs) == 10
+    assert len(progs) == 11
     uses_b = {_lib.OP[k] for k in ("AXPY", "MUL", "COPY")}
     for p in progs:
         assert len(p.ops) <= _lib.MAX_OPS, p.name
         assert len(p.arrs) <= _lib.MAX_ARR, p.name
         assert len(p.mats) <= _lib.MAX_MAT, p.name
         assert 1 <= p.nslots <= _lib.MAX_SLOTS
+        chain = {_lib.OP[k] for k in ("DIFF", "TDMA2", "FDMA")}
         for o in p.ops:
             assert 0 <= o.a < p.nslots, p.name
             if o.code in uses_b:
                 assert 0 <= o.b < p.nslots, p.name
+            if o.code in chain:
+                assert o.a + max(o.b, 1) <= p.nslots, p.name
+            if o.code == _lib.OP["FDMA"]:
+                assert o.mat + max(o.b, 1) <= len(p.mats)
             assert o.len < _lib.MAX_LEN and o.par < _lib.MAX_PAR
         # every array stored is either state or scratch; every loaded array is defined
         assert p.axis in (0, 1)
