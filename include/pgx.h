@@ -135,6 +135,17 @@ int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in,
              double* out, int64_t out_s0, int64_t out_s1, int32_t n_out,
              int32_t n, int32_t nlines, int32_t axis, int32_t mode, void* stream);
 
+/* Two-axis Chebyshev transform of an n0_in x n1_in array: axis 0 with the DCT-I of
+ * N0 points, then axis 1 with N1 points (FieldBase.forward / backward over both axes,
+ * field.py:14-56).  PGX_DCT_BWD: coefficients zero-padded to N0 x N1 -> values on the
+ * (3/2-dealiased) grid; PGX_DCT_FWD: values -> coefficients truncated to
+ * n0_out x n1_out after each axis.  `work` is caller-provided device scratch of at
+ * least n0_out * n1_in doubles holding the result of the axis-0 pass. */
+int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in_s1, int32_t n0_in, int32_t n1_in,
+                          double* out, int64_t out_s0, int64_t out_s1, int32_t n0_out, int32_t n1_out,
+                          int32_t N0, int32_t N1, int32_t mode, double* work, int64_t work_doubles,
+                          void* stream);
+
 /* Chebyshev derivative recurrence applied `count` times along axis, n points.
  * Replaces differentiate_cheby.diff_1d / diff_2d (differentiate_cheby.f90:1-53,
  * called at chebyshev.py:124,128). */

@@ -310,12 +310,12 @@ extern "C" int pgx_dct_table(int32_t n, const double** table) {
 }
 
 // ------------------------------------------------------------------- DCT-I
-extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, double* out, int64_t out_s0,
-                        int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
-                        void* stream) {
-  if (!in || !out || n < 2 || n > PGX_LMAX - 8 || n_in < 0 || n_in > n || n_out < 0 || n_out > n || nlines < 0 ||
-      axis < 0 || axis > 1 || mode < 0 || mode > 2)
-    return PGX_E_ARG;
+// One DCT-I pass along `axis`: `in` (n_in points along axis, zero-padded to n)
+// -> `out` (first n_out points).  `tab` is the twiddle table (fft) or the dense
+// scaled cosine matrix.
+int pgx_dct_pass(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, double* out, int64_t out_s0,
+                 int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
+                 const double* tab, bool fft, void* stream) {
   pgx_program P;
   pgx_instance I;
   init_prog(P, I, axis);
@@ -323,10 +323,6 @@ extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t 
   I.len[1] = n;
   set_axis_arr(I, 0, in, in_s0, in_s1, axis, n_in, nlines);
   set_axis_arr(I, 1, out, out_s0, out_s1, axis, n_out, nlines);
-  const double* tab = nullptr;
-  bool fft = fft_length_ok(2 * (n - 1));
-  int rc = fft ? twiddles(n, &tab) : dense_dct(n, mode, &tab);
-  if (rc) return rc;
   I.mat[0] = tab;
   P.nops = 3;
   P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
@@ -339,6 +335,41 @@ extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t 
   P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
   pick_tile(&P, nlines, n, 2, P.fft_n);
   return pgx_run(&P, &I, stream);
+}
+
+bool pgx_fft_length_ok(int n) { return fft_length_ok(2 * (n - 1)); }
+
+extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, double* out, int64_t out_s0,
+                        int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
+                        void* stream) {
+  if (!in || !out || n < 2 || n > PGX_LMAX - 8 || n_in < 0 || n_in > n || n_out < 0 || n_out > n || nlines < 0 ||
+      axis < 0 || axis > 1 || mode < 0 || mode > 2)
+    return PGX_E_ARG;
+  const double* tab = nullptr;
+  bool fft = fft_length_ok(2 * (n - 1));
+  int rc = fft ? twiddles(n, &tab) : dense_dct(n, mode, &tab);
+  if (rc) return rc;
+  return pgx_dct_pass(in, in_s0, in_s1, n_in, out, out_s0, out_s1, n_out, n, nlines, axis, mode, tab, fft, stream);
+}
+
+// Both axes: axis 0 (in -> work, n0_out x n1_in, row-major) then axis 1 (work -> out).
+extern "C" int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in_s1, int32_t n0_in, int32_t n1_in,
+                                     double* out, int64_t out_s0, int64_t out_s1, int32_t n0_out, int32_t n1_out,
+                                     int32_t N0, int32_t N1, int32_t mode, double* work, int64_t work_doubles,
+                                     void* stream) {
+  if (!in || !out || !work || mode < 0 || mode > 2 || N0 < 2 || N1 < 2 || N0 > PGX_LMAX - 8 || N1 > PGX_LMAX - 8 ||
+      n0_in < 0 || n0_in > N0 || n1_in < 0 || n1_in > N1 || n0_out < 0 || n0_out > N0 || n1_out < 0 || n1_out > N1)
+    return PGX_E_ARG;
+  if (work_doubles < (int64_t)n0_out * n1_in) return PGX_E_ARG;
+  const double* t0 = nullptr;
+  const double* t1 = nullptr;
+  bool f0 = fft_length_ok(2 * (N0 - 1)), f1 = fft_length_ok(2 * (N1 - 1));
+  int rc = f0 ? twiddles(N0, &t0) : dense_dct(N0, mode, &t0);
+  if (!rc) rc = f1 ? twiddles(N1, &t1) : dense_dct(N1, mode, &t1);
+  if (rc) return rc;
+  rc = pgx_dct_pass(in, in_s0, in_s1, n0_in, work, n1_in, 1, n0_out, N0, n1_in, 0, mode, t0, f0, stream);
+  if (rc) return rc;
+  return pgx_dct_pass(work, n1_in, 1, n1_in, out, out_s0, out_s1, n1_out, N1, n0_out, 1, mode, t1, f1, stream);
 }
 
 // ------------------------------------------------------- derivative recurrence

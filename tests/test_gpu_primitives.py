@@ -211,3 +211,33 @@ def test_rbc2d_plain_golden(pg, golden, case):
     assert abs(Nu - nu) / abs(nu) < 1e-8
     assert abs(Nuv - nuv) / abs(nuv) < 1e-8
     assert abs(ns.eval_KE() - ke) / abs(ke) < 1e-8
+
+
+@pytest.mark.parametrize("shape", [(33, 20), (65, 129)])
+def test_cheb_transform_2d_dealiased(pg, shape):
+    """pgx_cheb_transform_2d = deriv_field.dealias.backward / .forward (field.py:14-56) for CH x CH."""
+    import torch
+    from pypde_gb300 import _lib
+    from oracle import field as ofo
+    N, M = shape
+    Nd, Md = int(1.5 * N), int(1.5 * M)
+    sp2 = ofo.Space2D(("CH", "CH"), (N, M))
+    rng = np.random.default_rng(8)
+    c = rng.uniform(-1, 1, (N, M))
+    v = rng.uniform(-1, 1, (Nd, Md))
+    L = _lib.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    ct = torch.as_tensor(c, device="cuda")
+    out = torch.empty((Nd, Md), dtype=torch.float64, device="cuda")
+    work = torch.empty(Nd * M, dtype=torch.float64, device="cuda")
+    _lib.check(L.pgx_cheb_transform_2d(ct.data_ptr(), M, 1, N, M, out.data_ptr(), Md, 1, Nd, Md, Nd, Md,
+                                       _lib.DCT_BWD, work.data_ptr(), work.numel(), st))
+    assert rel_err(host(out), sp2.dealias_backward(c)) < TOL
+    vt = torch.as_tensor(v, device="cuda")
+    out2 = torch.empty((N, M), dtype=torch.float64, device="cuda")
+    work2 = torch.empty(N * Md, dtype=torch.float64, device="cuda")
+    _lib.check(L.pgx_cheb_transform_2d(vt.data_ptr(), Md, 1, Nd, Md, out2.data_ptr(), M, 1, N, M, Nd, Md,
+                                       _lib.DCT_FWD, work2.data_ptr(), work2.numel(), st))
+    assert rel_err(host(out2), sp2.dealias_forward(v)) < TOL
+    assert L.pgx_cheb_transform_2d(ct.data_ptr(), M, 1, N, M, out.data_ptr(), Md, 1, Nd, Md, Nd, Md,
+                                   _lib.DCT_BWD, work.data_ptr(), Nd * M - 1, st) == 1  # workspace too small
