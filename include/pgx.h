@@ -146,6 +146,25 @@ int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in_s1, int32_
                           int32_t N0, int32_t N1, int32_t mode, double* work, int64_t work_doubles,
                           void* stream);
 
+/* Zero-allocation variant of pgx_cheb_transform_2d.  No counterpart in the
+ * reference: it serves callers that cannot let a library allocate device memory
+ * (host codes that own all device memory through their own pool or budget, and
+ * time loops that must not hit the device-wide synchronisation of cudaMalloc /
+ * cudaFree).  Same arguments and results as pgx_cheb_transform_2d without `work`;
+ * the scratch between the two axis passes (at most PGX_NOALLOC_SCRATCH_DOUBLES =
+ * n0_out * n1_in doubles, 16 MiB) and the twiddle tables live in static device
+ * arrays that every GPU loading the library holds until exit.  Lengths N0, N1
+ * must have n-1 = 2^a 3^b (FFT plans only).  Larger or other sizes return
+ * PGX_E_ARG before any launch.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine.  The first call on a device looks up the arrays' device
+ * addresses (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the arrays and they keep the last call's contents:
+ * calls that overlap on the GPU race (keep them on one stream). */
+#define PGX_NOALLOC_SCRATCH_DOUBLES (1 << 21)
+int pgx_cheb_transform_2d_noalloc(const double* in, int64_t in_s0, int64_t in_s1, int32_t n0_in, int32_t n1_in,
+                                  double* out, int64_t out_s0, int64_t out_s1, int32_t n0_out, int32_t n1_out,
+                                  int32_t N0, int32_t N1, int32_t mode, void* stream);
+
 /* Chebyshev derivative recurrence applied `count` times along axis, n points.
  * Replaces differentiate_cheby.diff_1d / diff_2d (differentiate_cheby.f90:1-53,
  * called at chebyshev.py:124,128). */
