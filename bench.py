@@ -237,6 +237,7 @@ def run_gpu(args, rank, world):
     solvers, fb = build_batch(specs)
     n_inst = len(solvers)
     stream = torch.cuda.current_stream()
+    tuned = fb.autotune() if not args.no_tune else None
     fb.capture(1)
     state_bytes = fb.state_arena.numel() * 8
     work_bytes = fb.scratch_bytes()
@@ -317,6 +318,8 @@ def run_gpu(args, rank, world):
         per = []
         for i in range(n_inst):
             one = fb.single(i)
+            if not args.no_tune:
+                one.autotune(reps=2)
             one.capture(1)
             for _ in range(2):
                 one.step()
@@ -365,6 +368,7 @@ def run_gpu(args, rank, world):
         "passes": passes,
         "plain": plain,
         "eager": eager,
+        "autotuned_tiles": tuned,
         "finite_instances": finite,
         "host_wall_s": round(wall, 3),
     }
@@ -419,6 +423,7 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -590,6 +590,38 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     return tb, min(nt, 1024)
 
 
+def _candidates(prog, lines_total, lcap, fft_n, max_lines):
+    """Tile shapes the autotuner tries for one pass: lines per CTA chosen so that 1, 2, 3
+    or 4 CTAs fit an SM's shared memory, plus small tiles for short passes."""
+    nbuf = prog.nslots + 1
+    per_line = 8 * nbuf * lcap + (32 * (fft_n - 1) if fft_n > 1 else 0)
+    width = 1
+    for o in prog.ops:
+        if o.code in (_lib.OP["FDMA"], _lib.OP["TDMA2"], _lib.OP["POISSON"]):
+            width = max(width, 2 * max(o.b, 1))
+        elif o.code == _lib.OP["DIFF"]:
+            width = max(width, max(o.b, 1))
+    tbs = set()
+    for ctas in (1, 2, 3, 4):
+        tb = (SMEM_PER_SM // ctas - 2048) // per_line
+        tbs.add(int(tb))
+    tbs.update({4, 8, 16})
+    out = []
+    for tb in sorted(tbs):
+        tb = min(tb, 64, max(max_lines, 1))
+        if fft_n > 1:
+            tb -= tb % 2
+            if tb < 2:
+                continue
+        if tb < 1 or tb * per_line > SMEM_PER_SM - 2048:
+            continue
+        for nt in (256, 512):
+            nt = max(nt, 32 * -(-width * tb // 32))
+            if nt <= 1024 and (tb, nt) not in out:
+                out.append((tb, nt))
+    return out
+
+
 class FusedBatch:
     """Fused Euler step for a batch of NavierStokes instances (any sizes / Ra)."""
 
@@ -616,30 +648,77 @@ class FusedBatch:
         self._build_launches()
         self.graph = None
 
-    def _build_launches(self):
+    def _pass_geometry(self, prog):
+        lines = [I.lines(prog) for I in self.insts]
+        maxlen = max(program_maxlen(prog, I.lens) for I in self.insts)
+        lcap = (maxlen + 1) | 1
+        fft_n = max(I.lens[L_ND + prog.axis] for I in self.insts) if (prog.has_dct and self.fft) else 0
+        return lines, lcap, fft_n
+
+    def _launch(self, prog, tb, nt, d_insts=None):
         dev = device()
-        self.launches = []
-        for prog in self.progs:
-            lines = [I.lines(prog) for I in self.insts]
-            maxlen = max(program_maxlen(prog, I.lens) for I in self.insts)
-            lcap = (maxlen + 1) | 1
-            fft_n = max(I.lens[L_ND + prog.axis] for I in self.insts) if (prog.has_dct and self.fft) else 0
-            tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
-            P = _lib.PgxProgram()
-            P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
-            P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
-            assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
-            for i, o in enumerate(prog.ops):
-                P.ops[i] = o
+        lines, lcap, fft_n = self._pass_geometry(prog)
+        P = _lib.PgxProgram()
+        P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
+        P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
+        assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
+        for i, o in enumerate(prog.ops):
+            P.ops[i] = o
+        if d_insts is None:
             insts = (_lib.PgxInstance * len(self.insts))()
             for k, I in enumerate(self.insts):
                 I.fill(prog, insts[k])
             d_insts = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(dev)
-            work = []
-            for k, nl in enumerate(lines):
-                work += [(k, t) for t in range(-(-nl // tb))]
-            d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=dev)
-            self.launches.append((prog.name, P, d_insts, d_work, len(work)))
+        work = []
+        for k, nl in enumerate(lines):
+            work += [(k, t) for t in range(-(-nl // tb))]
+        d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=dev)
+        return (prog.name, P, d_insts, d_work, len(work))
+
+    def _build_launches(self):
+        self.launches = []
+        for prog in self.progs:
+            lines, lcap, fft_n = self._pass_geometry(prog)
+            tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
+            self.launches.append(self._launch(prog, tb, nt))
+
+    def autotune(self, reps=3, verbose=False):
+        """Time every candidate tile shape of every pass on this batch and keep the fastest.
+
+        The passes update the state in place, so the state is saved before and
+        restored after tuning.  Returns {pass: (lines per CTA, threads, ms)}.
+        """
+        saved = [{k: I.arrays[k].clone() for k in _Instance.STATE} for I in self.insts]
+        stream = torch.cuda.current_stream()
+        chosen = {}
+        for i, prog in enumerate(self.progs):
+            lines, lcap, fft_n = self._pass_geometry(prog)
+            best = None
+            d_insts = self.launches[i][2]
+            for tb, nt in _candidates(prog, sum(lines), lcap, fft_n, max(lines)):
+                L = self._launch(prog, tb, nt, d_insts)
+                self.launches[i] = L
+                self.run_pass(i)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(reps):
+                    self.run_pass(i)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / reps
+                if verbose:
+                    print(prog.name, tb, nt, round(ms, 4))
+                if best is None or ms < best[0]:
+                    best = (ms, L, tb, nt)
+            self.launches[i] = best[1]
+            chosen[prog.name] = (best[2], best[3], round(best[0], 4))
+        for I, s in zip(self.insts, saved):
+            for k, v in s.items():
+                I.arrays[k].copy_(v)
+        torch.cuda.synchronize()
+        self.graph = None
+        self.tuned = chosen
+        return chosen
 
     def run_pass(self, i):
         name, P, d_insts, d_work, nwork = self.launches[i]

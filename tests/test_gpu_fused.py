@@ -118,6 +118,8 @@ def test_batched_heterogeneous(NS):
         ns.set_temperature_noise(seed, 1e-3)
         solvers.append(ns)
     fb = FusedBatch(solvers)
+    tuned = fb.autotune(reps=1)
+    assert set(tuned) == {p.name for p in fb.progs}
     fb.capture(1)
     for _ in range(3):
         fb.step()
