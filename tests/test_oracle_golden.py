@@ -140,3 +140,17 @@ def test_rbc2d_steps(golden, case):
     assert abs(ns.eval_Nu() - nu) / abs(nu) < 1e-10
     assert abs(ns.eval_Nuvol() - nuv) / abs(nuv) < 1e-10
     assert abs(ns.eval_KE() - ke) / abs(ke) < 1e-8
+
+
+def test_adjoint_step(golden):
+    """One adjoint-descent step (navier/rbc2d_adj.py) against the reference's own output."""
+    from oracle import rbc2d_adj as oadj
+    nsa = oadj.NavierStokesAdjoint(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, tsave=None,
+                                   dealias=True, integrator="eu", beta=1.0)
+    noise = 1e-2 * np.random.default_rng(7).uniform(-1, 1, (33, 33))
+    nsa.That = nsa.Tsp.forward(noise)
+    assert rel_err(nsa.That, golden["adj33_T0"]) < TOL
+    nsa.update()
+    for name, arr in (("T1", nsa.That), ("U1", nsa.Uhat), ("V1", nsa.Vhat), ("FT", nsa.FT), ("FU", nsa.FU),
+                      ("FV", nsa.FV), ("TA", nsa.TA), ("UA", nsa.UA), ("VA", nsa.VA)):
+        assert rel_err(arr, golden["adj33_" + name]) < 1e-9, name
