@@ -260,7 +260,9 @@ int round_odd(int x) { return x | 1; }
 // Lines per CTA and CTA size for a single-instance pass.
 void pick_tile(pgx_program* P, int nlines, int maxlen, int nbuf, int fft_n) {
   P->lcap = round_odd(maxlen + 1);
-  int64_t per_line = (int64_t)8 * nbuf * P->lcap + (fft_n > 1 ? (int64_t)32 * (fft_n - 1) : 0);
+  // FFT buffers: 2 buffers x stride complex per line pair (see pgx_fft_stride)
+  int64_t stride = fft_n > 1 ? (((fft_n - 1) & 1) == 0 ? fft_n - 1 : 2 * (fft_n - 1)) : 0;
+  int64_t per_line = (int64_t)8 * nbuf * P->lcap + 16 * stride + 8;
   int64_t budget = smem_optin_max() - 4096;
   int tbmax = (int)(budget / per_line);
   if (tbmax < 1) tbmax = 1;

@@ -21,6 +21,13 @@
 
 #include "pgx.h"
 
+// Complex elements per line pair in each FFT buffer for DCT lengths up to n:
+// n - 1 for the folded algorithm (even n - 1), 2(n - 1) for paired lines.
+__host__ __device__ inline int pgx_fft_stride(int n) {
+  if (n <= 1) return 0;
+  return ((n - 1) & 1) == 0 ? (n - 1) : 2 * (n - 1);
+}
+
 namespace pgx {
 
 // 2k for k < PGX_LMAX: multipliers of the derivative recurrence, read through
@@ -39,6 +46,7 @@ struct Ctx {
   double* sm;       // slot buffers
   double2* f0;      // FFT ping buffer
   double2* f1;      // FFT pong buffer
+  double* ybuf;     // one scalar per line (DCT-I: y_1 of the folded algorithm)
   int tb, lcap, nthreads, tid;
   int fft_stride;   // complex elements per pair in the FFT buffers
   int l0, nlines;   // first line of the tile, lines of the instance
@@ -261,28 +269,46 @@ __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
 }
 
-// Chebyshev derivative in place (differentiate_cheby.f90:28-53), one thread per
-// (slot, line), both parity chains interleaved:
-//   dc_{n-1} = 0, dc_j = dc_{j+2} + 2(j+1) c_{j+1} (j = n-2..1), dc_0 = dc_2/2 + c_1.
-// c_{j+1} is kept in a register before its slot entry is overwritten.
+// Chebyshev derivative in place (differentiate_cheby.f90:28-53):
+//   dc_{n-1} = 0, dc_j = dc_{j+2} + 2(j+1) c_{j+1} (j = n-2..1), dc_0 = dc_2/2 + c_1,
+// i.e. dc_j = S_{(j+1) mod 2}(j+1) with S_p(i) = sum_{k >= i, k = p mod 2} 2k c_k.
+// One warp per (slot, line): each lane owns a contiguous chunk, the chunk totals of
+// both parity classes are suffix-scanned across the warp, then every lane walks its
+// chunk backwards.  Depth ~ n/32 + 5 dependent adds instead of n.
 __device__ void op_diff(Ctx& c, const pgx_op& op) {
   const int ns = nslot_of(op);
-  for (int w = c.tid; w < ns * c.tb; w += c.nthreads) {
+  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+  for (int w = warp; w < ns * c.tb; w += nw) {
     const int s = w / c.tb, t = w - s * c.tb;
     const int n = c.slen[op.a + s];
     double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    const int chunk = (n + 31) >> 5;
+    const int a = lane * chunk, b = min(a + chunk, n);
     for (int rep = 0; rep < op.k; ++rep) {
-      double acc[2] = {0.0, 0.0};
-      double cnext = x[n - 1];  // c_{j+1}
-      x[n - 1] = 0.0;
-      for (int j = n - 2; j >= 1; --j) {
-        const double cj = x[j];
-        const double v = fma(c_twok.v[j + 1], cnext, acc[j & 1]);
-        acc[j & 1] = v;
-        x[j] = v;
-        cnext = cj;
+      double tot[2] = {0.0, 0.0};
+      for (int i = a; i < b; ++i) tot[i & 1] = fma(c_twok.v[i], x[i], tot[i & 1]);
+      const double c1 = x[1];
+      // exclusive suffix sums of the chunk totals over the lanes above this one
+      double in0 = tot[0], in1 = tot[1];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double v0 = __shfl_down_sync(0xffffffffu, in0, o);
+        const double v1 = __shfl_down_sync(0xffffffffu, in1, o);
+        if (lane + o < 32) {
+          in0 += v0;
+          in1 += v1;
+        }
       }
-      x[0] = fma(0.5, acc[0], cnext);  // dc_2 / 2 + c_1
+      double acc[2] = {in0 - tot[0], in1 - tot[1]};  // S_p(b)
+      __syncwarp();
+      for (int i = b - 1; i >= a; --i) {
+        const double wi = c_twok.v[i] * x[i];
+        x[i] = acc[(i + 1) & 1];  // dc_i = S_{(i+1) mod 2}(i+1)
+        acc[i & 1] += wi;
+      }
+      __syncwarp();
+      if (lane == 0) x[0] = fma(0.5, n > 2 ? x[2] : 0.0, c1);
+      __syncwarp();
     }
   }
 }
@@ -398,9 +424,9 @@ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_doub
 //          forward post-scale (no extraction pass).
 template <int R, bool FIRST, bool LAST>
 __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src, double2* dst, const double2* tw,
-                                               int L, int Ns, int npairs, double* x, int mode) {
+                                               int L, int Ns, int npairs, double* x, int mode, int tws = 1) {
   const int LR = L / R;
-  const int step = L / (Ns * R);
+  const int step = tws * (L / (Ns * R));  // twiddle table holds exp(-2 pi i k / (tws L))
   const int N = L >> 1;
   const double invN = 1.0 / N;
   for (int idx = c.tid; idx < npairs * LR; idx += c.nthreads) {
@@ -476,19 +502,151 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
   }
 }
 
+__device__ __forceinline__ void x_nan(const Ctx& c, int slot, int idx, int n) {
+  int t = idx / n, k = idx - t * n;
+  slot_ptr(c, slot)[t * c.lcap + k] = __longlong_as_double(0x7ff8000000000000ULL);
+}
+
 __device__ __forceinline__ int next_radix(int rem) { return (rem & 3) == 0 ? 4 : ((rem & 1) == 0 ? 2 : 3); }
 
 template <bool FIRST, bool LAST>
 __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double2* src, double2* dst, const double2* tw,
-                                               int L, int Ns, int npairs, double* x, int mode) {
-  if (R == 4) stockham_stage<4, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
-  else if (R == 2) stockham_stage<2, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
-  else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode);
+                                               int L, int Ns, int npairs, double* x, int mode, int tws = 1) {
+  if (R == 4) stockham_stage<4, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
+  else if (R == 2) stockham_stage<2, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
+  else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
 }
 
-// DCT-I of the slot (length n) in place, see stockham_stage for the data path.
+// DCT-I for even N = n - 1, exploiting both the realness and the even symmetry
+// of the extension (half the FFT length of the paired approach):
+//   fold   u_j = (x_j + x_{N-j})/2 - sin(pi j/N) (x_j - x_{N-j}),  j = 0..N-1
+//          y_1 = (x_0 - x_N) + 2 sum_{0<j<N/2} (x_j - x_{N-j}) cos(pi j/N)
+//   FFT    Z = DFT_N(u_a + i u_b) for the two lines (a, b) of a pair
+//   untangle  y_{2m} = Z_m + conj(Z_{N-m}) (real / imag part for line a / b),
+//          odd increments y_{2m+1} - y_{2m-1} = Im(Z_{N-m} - Z_m) (a), Re(Z_m - Z_{N-m}) (b)
+//   scan   y_{2m+1} = y_1 + sum of increments (one warp per line).
+// tw is the table exp(-2 pi i k / (2N)): W_N^k = tw[2k], (cos, -sin)(pi j / N) = tw[j].
+// The backward pre-scale (-1)^j w_j is common to x_j and x_{N-j} (N even) and
+// applied to u_j, d_j; the forward post-scale to the outputs.
+__device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int n = c.slen[op.a];
+  const int N = n - 1, H = N / 2;
+  const int mode = op.k;
+  const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
+  double* x = slot_ptr(c, op.a);
+  const int npairs = (c.tb + 1) >> 1;
+  const double invN = 1.0 / N;
+  // fold
+  for (int idx = c.tid; idx < npairs * N; idx += c.nthreads) {
+    const int pr = idx / N, j = idx - pr * N;
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
+    const double sn = -__ldg(&tw[j].y);
+    double sg = 1.0;
+    if (mode == PGX_DCT_BWD && j > 0) sg = (j & 1) ? -0.5 : 0.5;
+    const double a0 = x[t0 * c.lcap + j], a1 = x[t0 * c.lcap + N - j];
+    double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
+    double ub = 0.0;
+    if (two) {
+      const double b0 = x[(t0 + 1) * c.lcap + j], b1 = x[(t0 + 1) * c.lcap + N - j];
+      ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
+    }
+    if (mode == PGX_DCT_BWD) {
+      ua *= sg;
+      ub *= sg;
+    }
+    c.f0[pr * c.fft_stride + j] = make_double2(ua, ub);
+  }
+  // y_1: one warp per line
+  {
+    const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+    for (int t = warp; t < c.tb; t += nw) {
+      const double* xl = x + t * c.lcap;
+      double acc = 0.0;
+      for (int j = 1 + lane; j < H; j += 32) {
+        double d = xl[j] - xl[N - j];
+        if (mode == PGX_DCT_BWD) d *= (j & 1) ? -0.5 : 0.5;
+        acc = fma(__ldg(&tw[j].x), d, acc);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) c.ybuf[t] = fma(2.0, acc, xl[0] - xl[N]);
+    }
+  }
+  __syncthreads();
+  // FFT of length N over the pairs
+  double2* bufs[2] = {c.f0, c.f1};
+  int cur = 0, Ns = 1;
+  for (int rem = N; rem > 1;) {
+    const int R = next_radix(rem);
+    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, npairs, x, mode, 2);
+    cur ^= 1;
+    Ns *= R;
+    rem /= R;
+    __syncthreads();
+  }
+  const double2* Z = bufs[cur];
+  // untangle: even outputs, odd increments
+  for (int idx = c.tid; idx < npairs * (H + 1); idx += c.nthreads) {
+    const int pr = idx / (H + 1), m = idx - pr * (H + 1);
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
+    const double2 zm = Z[pr * c.fft_stride + m];
+    const double2 zn = Z[pr * c.fft_stride + (m == 0 ? 0 : N - m)];
+    double ya = zm.x + zn.x, yb = zm.y + zn.y;
+    if (mode == PGX_DCT_FWD) {
+      const double sc = (m == 0 || m == H) ? 0.5 * invN : invN;  // (-1)^{2m} = 1
+      ya *= sc;
+      yb *= sc;
+    }
+    x[t0 * c.lcap + 2 * m] = ya;
+    if (two) x[(t0 + 1) * c.lcap + 2 * m] = yb;
+    if (m >= 1 && m < H) {
+      x[t0 * c.lcap + 2 * m + 1] = zn.y - zm.y;
+      if (two) x[(t0 + 1) * c.lcap + 2 * m + 1] = zm.x - zn.x;
+    } else if (m == 0) {
+      x[t0 * c.lcap + 1] = c.ybuf[t0];
+      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[t0 + 1];
+    }
+  }
+  __syncthreads();
+  // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1 (one warp per line)
+  {
+    const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+    const int chunk = (H + 31) / 32;
+    const double osc = mode == PGX_DCT_FWD ? -invN : 1.0;  // odd k: (-1)^k / N
+    for (int t = warp; t < c.tb; t += nw) {
+      double* xl = x + t * c.lcap;
+      const int m0 = lane * chunk, m1 = min(m0 + chunk, H);
+      double run = 0.0;
+      for (int m = m0; m < m1; ++m) run += xl[2 * m + 1];
+      double incl = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        double v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      double pre = incl - run;  // exclusive prefix of this lane's chunk
+      for (int m = m0; m < m1; ++m) {
+        pre += xl[2 * m + 1];
+        xl[2 * m + 1] = pre * osc;
+      }
+    }
+  }
+}
+
+// DCT-I of the slot (length n) in place: the folded half-length algorithm for
+// even n - 1, otherwise paired lines through a length-2(n-1) FFT (stockham_stage).
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
+  if (((n - 1) & 1) == 0 && n >= 3) {
+    op_dct_even(c, op, I);
+    return;
+  }
+  if (2 * (n - 1) > c.fft_stride) {  // buffer sized for a shorter even length: refuse loudly
+    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a, idx, n);
+    return;
+  }
   const int N = n - 1, L = 2 * N;
   const int mode = op.k;
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
@@ -552,9 +710,10 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   const int nbuf = P.nslots + 1;
   c.sm = BATCHED ? smem_dyn + (sizeof(pgx_instance) + 7) / 8 : smem_dyn;
   size_t off = (size_t)nbuf * c.tb * c.lcap;
-  c.fft_stride = P.fft_n > 1 ? 2 * (P.fft_n - 1) : 0;
+  c.fft_stride = pgx_fft_stride(P.fft_n);
   c.f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
   c.f1 = c.f0 + (size_t)((c.tb + 1) >> 1) * c.fft_stride;
+  c.ybuf = reinterpret_cast<double*>(c.f1 + (size_t)((c.tb + 1) >> 1) * c.fft_stride);
   for (int s = 0; s < nbuf; ++s) c.phys[s] = s;
   for (int s = 0; s < PGX_MAX_SLOTS; ++s) c.slen[s] = 0;
   c.spare = P.nslots;
@@ -619,7 +778,7 @@ extern "C" int64_t pgx_program_smem(const pgx_program* P) {
   int64_t nbuf = P->nslots + 1;
   int64_t doubles = nbuf * P->tb * P->lcap;
   doubles += doubles & 1;
-  if (P->fft_n > 1) doubles += 2 * 2 * (int64_t)((P->tb + 1) / 2) * 2 * (P->fft_n - 1);
+  if (P->fft_n > 1) doubles += 2 * 2 * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + P->tb + 1;
   return doubles * 8;
 }
 

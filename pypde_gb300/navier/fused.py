@@ -549,6 +549,15 @@ def program_maxlen(prog, lens):
 
 
 CHAIN_OPS = ("FDMA", "POISSON", "TDMA2")
+
+
+def fft_bytes_per_line(fft_n):
+    """Shared memory of the DCT-I work buffers per line: two buffers of n-1 (folded algorithm,
+    even n-1) or 2(n-1) (paired lines) complex values per pair of lines, plus one scalar."""
+    if fft_n <= 1:
+        return 0
+    stride = fft_n - 1 if (fft_n - 1) % 2 == 0 else 2 * (fft_n - 1)
+    return 16 * stride + 8
 SMEM_PER_SM = 227 * 1024
 
 
@@ -562,7 +571,7 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     warp of chains.
     """
     nbuf = prog.nslots + 1
-    per_line = 8 * nbuf * lcap + (32 * (fft_n - 1) if fft_n > 1 else 0)
+    per_line = 8 * nbuf * lcap + fft_bytes_per_line(fft_n)
     chains = any(o.code in [_lib.OP[k] for k in CHAIN_OPS] for o in prog.ops)
     if fft_n > 1:
         budget = SMEM_PER_SM // 2 - 2048
@@ -594,7 +603,7 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     """Tile shapes the autotuner tries for one pass: lines per CTA chosen so that 1, 2, 3
     or 4 CTAs fit an SM's shared memory, plus small tiles for short passes."""
     nbuf = prog.nslots + 1
-    per_line = 8 * nbuf * lcap + (32 * (fft_n - 1) if fft_n > 1 else 0)
+    per_line = 8 * nbuf * lcap + fft_bytes_per_line(fft_n)
     width = 1
     for o in prog.ops:
         if o.code in (_lib.OP["FDMA"], _lib.OP["TDMA2"], _lib.OP["POISSON"]):

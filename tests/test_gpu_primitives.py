@@ -48,7 +48,7 @@ def test_galerkin_golden(pg, golden, N, key):
     assert rel_err(host(B.derivative(v, 2)), golden[f"{key}{N}_d2"]) < TOL
 
 
-@pytest.mark.parametrize("n", [33, 49, 65, 97, 129, 193, 257, 385, 513, 769, 1025, 17, 50])
+@pytest.mark.parametrize("n", [33, 49, 65, 97, 129, 193, 257, 385, 513, 769, 1025, 17, 50, 28, 5, 3])
 @pytest.mark.parametrize("axis", [0, 1])
 def test_dct_sizes_vs_oracle(pg, n, axis):
     """Microbench sizes (N = 33..1025, seed 1) and their 3/2-dealiased lengths, both axes;
