@@ -87,10 +87,14 @@ enum pgx_opcode {
   PGX_OP_DENSE = 18,    /* slot a = A slot a; A is len x slen row-major       */
   PGX_OP_FDMA = 19,     /* in-place -2/0/+2/+4 LU solve of slots a..a+b-1, table mat+s: [l|dinv|u1|u2] */
   PGX_OP_POISSON = 20,  /* like FDMA with per-line factors (line j at j*4*n)  */
-  PGX_OP_ZERO00 = 21    /* element 0 of the instance's line 0 = 0            */
+  PGX_OP_ZERO00 = 21,   /* element 0 of the instance's line 0 = 0            */
+  PGX_OP_DIFF_T = 22,   /* slots a..a+b-1 = (D^T)^k slot (adjoint of DIFF)   */
+  PGX_OP_FDMA_T = 23,   /* A^T x = b with the FDMA factors (adjoint of FDMA) */
+  PGX_OP_POISSON_T = 24 /* per-line transposed sweep (adjoint of POISSON)    */
 };
 
-enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2 };
+/* DCT modes; FWD_T and BWD_T are the exact transposes (adjoints) of FWD and BWD. */
+enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_FWD_T = 3, PGX_DCT_BWD_T = 4 };
 
 /* Chain ops (DIFF, TDMA2, FDMA) act on the b consecutive slots a..a+b-1 at
  * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset. */
@@ -129,6 +133,7 @@ int pgx_run_batched(const pgx_program* prog, const pgx_instance* d_insts,
  * mode PGX_DCT_RAW : scipy.fftpack.dctn(f, type=1, axes=(axis,))  (chebyshev.py:85-93)
  * mode PGX_DCT_FWD : Chebyshev.forward_fft incl. solve_mass       (chebyshev.py:67-76,143-149)
  * mode PGX_DCT_BWD : Chebyshev.backward_fft                         (chebyshev.py:78-83)
+ * mode PGX_DCT_FWD_T / PGX_DCT_BWD_T : the transposes of FWD / BWD (adjoints for reverse mode)
  * n_in <= n zero-pads the input along axis (pypde zero_pad, bases/utils.py:88-109);
  * n_out <= n truncates the output (zero_unpad, bases/utils.py:112-115). */
 int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in,
@@ -172,6 +177,12 @@ int pgx_cheb_diff(const double* c, int64_t c_s0, int64_t c_s1,
                   double* dc, int64_t dc_s0, int64_t dc_s1,
                   int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream);
 
+/* Transpose (adjoint) of pgx_cheb_diff: (D^T)^count along axis.  No reference counterpart:
+ * the backward of the derivative for reverse-mode differentiation of the time step. */
+int pgx_cheb_diff_t(const double* c, int64_t c_s0, int64_t c_s1,
+                    double* dc, int64_t dc_s0, int64_t dc_s1,
+                    int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream);
+
 /* Stencil plans: Galerkin <-> Chebyshev for ChebDirichlet ("CD") / ChebNeumann
  * ("CN") of N points (chebyshev.py:287-337, 382-392, 426-436). */
 typedef struct pgx_stencil_plan pgx_stencil_plan;
@@ -188,6 +199,17 @@ int pgx_stencil_from_chebyshev(const pgx_stencil_plan* plan,
                                const double* in, int64_t in_s0, int64_t in_s1,
                                double* out, int64_t out_s0, int64_t out_s1,
                                int32_t nlines, int32_t axis, void* stream);
+
+/* Transposes of the two stencil maps, for reverse mode (no reference counterpart):
+ * S^T (in N points, out N-2) and S (S^T S)^-1 (in N-2 points, out N). */
+int pgx_stencil_transpose(const pgx_stencil_plan* plan,
+                          const double* in, int64_t in_s0, int64_t in_s1,
+                          double* out, int64_t out_s0, int64_t out_s1,
+                          int32_t nlines, int32_t axis, void* stream);
+int pgx_stencil_from_chebyshev_t(const pgx_stencil_plan* plan,
+                                 const double* in, int64_t in_s0, int64_t in_s1,
+                                 double* out, int64_t out_s0, int64_t out_s1,
+                                 int32_t nlines, int32_t axis, void* stream);
 
 /* Offset-k tridiagonal solve, k = 2 (tdma.solve_tdma_1d/_2d, tdma.f90:2-107,
  * called from tdma.py:92-100).  a (n-2), b (n), c (n-2) are HOST arrays. */
@@ -209,6 +231,10 @@ int pgx_fdma_plan_destroy(pgx_fdma_plan* plan);
 int pgx_fdma_solve(const pgx_fdma_plan* plan, double* x, int64_t s0, int64_t s1,
                    int32_t nlines, int32_t axis, void* stream);
 
+/* Transposed solve A^T x = b with the same plan (adjoint of pgx_fdma_solve), in place. */
+int pgx_fdma_solve_t(const pgx_fdma_plan* plan, double* x, int64_t s0, int64_t s1,
+                     int32_t nlines, int32_t axis, void* stream);
+
 /* Upper offset-2 bidiagonal back substitution (twodma.solve_twodma_1d/_2d,
  * twodma.f90:2-62, plans.py:160-172): d (n), u (n-2) HOST diagonals; in place. */
 int pgx_twodma_plan_create(const double* d, const double* u, int32_t n, pgx_fdma_plan** plan);
@@ -226,6 +252,10 @@ int pgx_poisson_plan_destroy(pgx_poisson_plan* plan);
 /* axis 0: line j is column j (the reference's call path); axis 1: line j is row j. */
 int pgx_poisson_solve(const pgx_poisson_plan* plan, double* x, int64_t s0, int64_t s1,
                       int32_t axis, void* stream);
+
+/* Transposed per-line sweep (adjoint of pgx_poisson_solve), in place. */
+int pgx_poisson_solve_t(const pgx_poisson_plan* plan, double* x, int64_t s0, int64_t s1,
+                        int32_t axis, void* stream);
 
 /* Matrix applied along an axis, out = A in (MatrixBase.dot, matrix.py:41-56, used by
  * PlanRHS, plans.py:54-74).  A (rows x cols, row-major HOST) is stored banded when

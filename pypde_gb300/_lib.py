@@ -15,8 +15,8 @@ MAX_ARR, MAX_MAT, MAX_LEN, MAX_PAR, MAX_OPS, MAX_SLOTS, LMAX = 24, 16, 16, 16, 9
 
 OP = dict(LOAD=1, LOAD_ADD=2, LOAD_MUL=3, STORE=4, STORE_ADD=5, SCALE=6, AXPY=7, MUL=8, COPY=9,
           SETLEN=10, STENCIL=11, STENCIL_T=12, TDMA2=13, DIFF=14, DCT=15, BANDED=17, DENSE=18,
-          FDMA=19, POISSON=20, ZERO00=21)
-DCT_RAW, DCT_FWD, DCT_BWD = 0, 1, 2
+          FDMA=19, POISSON=20, ZERO00=21, DIFF_T=22, FDMA_T=23, POISSON_T=24)
+DCT_RAW, DCT_FWD, DCT_BWD, DCT_FWD_T, DCT_BWD_T = 0, 1, 2, 3, 4
 
 
 class PgxArray(ctypes.Structure):
@@ -68,6 +68,13 @@ SIGNATURES = {
     "pgx_cheb_diff": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                                      ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "pgx_cheb_diff_t": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                       ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "pgx_fdma_solve_t": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "pgx_poisson_solve_t": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int32, ctypes.c_void_p]),
     "pgx_stencil_plan_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_void_p]),
     "pgx_stencil_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pgx_stencil_to_chebyshev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
@@ -76,6 +83,12 @@ SIGNATURES = {
     "pgx_stencil_from_chebyshev": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                                   ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                                   ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "pgx_stencil_transpose": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                             ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.c_void_p]),
+    "pgx_stencil_from_chebyshev_t": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                                    ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
     "pgx_tdma_plan_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                             ctypes.c_int32, ctypes.c_void_p]),
     "pgx_tdma_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -10,9 +10,11 @@ import ctypes
 
 import numpy as np
 import scipy.sparse
+import torch
 
 from . import _lib
 from ._dev import empty_like_axis, geom, stream, to_dev
+from .autodiff import linear
 from .host import (dealias_size, gauss_lobatto, pseudoinverse_d2, stencil_matrix)
 
 
@@ -95,16 +97,31 @@ class Chebyshev(MetaBase):
         self.id = "CH"
         self.family_id = "CH"
 
-    def _dct(self, f, mode, n_out=None):
-        f = _along0(f)
+    _DCT_T = {_lib.DCT_FWD: _lib.DCT_FWD_T, _lib.DCT_BWD: _lib.DCT_BWD_T,
+              _lib.DCT_FWD_T: _lib.DCT_FWD, _lib.DCT_BWD_T: _lib.DCT_BWD}
+
+    def _dct_raw(self, f, mode, n_out):
         n_in = f.shape[0]
-        if n_in > self.N:
-            raise ValueError("input longer than the base")
-        out = empty_like_axis(f, 0, self.N if n_out is None else n_out)
+        if n_in > self.N or n_out > self.N:
+            raise ValueError("input or output longer than the base")
+        out = empty_like_axis(f, 0, n_out)
         p, s0, s1, _, nl = geom(f, 0)
         q, t0, t1, no, _ = geom(out, 0)
         _lib.check(_lib.lib().pgx_dct1(p, s0, s1, n_in, q, t0, t1, no, self.N, nl, 0, mode, stream()), "dct1")
         return out
+
+    def _dct(self, f, mode, n_out=None):
+        """DCT of mode ``mode`` along axis 0; input zero-padded and output truncated to n_out.
+
+        Differentiable: the transpose is the transposed mode with the lengths swapped."""
+        f = _along0(f)
+        n_in, n_out = f.shape[0], self.N if n_out is None else n_out
+        if mode == _lib.DCT_RAW:
+            if f.requires_grad and torch.is_grad_enabled():
+                raise NotImplementedError("dctn is not differentiable; use forward_fft / backward_fft")
+            return self._dct_raw(f, mode, n_out)
+        mt = self._DCT_T[mode]
+        return linear(f, lambda x: self._dct_raw(x, mode, n_out), lambda g: self._dct_raw(g, mt, n_in))
 
     def forward_fft(self, f, mass=True):
         """Physical -> Chebyshev coefficients (chebyshev.py:67-76)."""
@@ -127,11 +144,15 @@ class Chebyshev(MetaBase):
         """Chebyshev recurrence applied ``deriv`` times (chebyshev.py:117-131)."""
         if deriv == 0:
             return fhat
-        f = _along0(fhat)
+        return linear(_along0(fhat), lambda x: self._diff(x, deriv, "pgx_cheb_diff"),
+                      lambda g: self._diff(g, deriv, "pgx_cheb_diff_t"))
+
+    @staticmethod
+    def _diff(f, deriv, fn):
         out = empty_like_axis(f, 0, f.shape[0])
         p, s0, s1, n, nl = geom(f, 0)
         q, t0, t1, _, _ = geom(out, 0)
-        _lib.check(_lib.lib().pgx_cheb_diff(p, s0, s1, q, t0, t1, n, nl, 0, deriv, stream()), "cheb_diff")
+        _lib.check(getattr(_lib.lib(), fn)(p, s0, s1, q, t0, t1, n, nl, 0, deriv, stream()), fn)
         return out
 
     def solve_mass(self, f):
@@ -204,27 +225,26 @@ class GalerkinChebyshev(MetaBase):
             u = u + self.bc.to_chebyshev(bc)
         return self.family.backward_fft(u)
 
-    def to_chebyshev(self, vhat):
-        """u = S v (chebyshev.py:287-293)."""
-        v = _along0(vhat)
-        assert v.shape[0] == self.M, "{} {}".format(v.shape[0], self.M)
-        out = empty_like_axis(v, 0, self.N)
-        p, s0, s1, _, nl = geom(v, 0)
+    def _stencil_op(self, x, fn, n_out):
+        out = empty_like_axis(x, 0, n_out)
+        p, s0, s1, _, nl = geom(x, 0)
         q, t0, t1, _, _ = geom(out, 0)
-        _lib.check(_lib.lib().pgx_stencil_to_chebyshev(self._plan.h, p, s0, s1, q, t0, t1, nl, 0, stream()),
-                   "to_chebyshev")
+        _lib.check(getattr(_lib.lib(), fn)(self._plan.h, p, s0, s1, q, t0, t1, nl, 0, stream()), fn)
         return out
 
+    def to_chebyshev(self, vhat):
+        """u = S v (chebyshev.py:287-293); transpose S^T."""
+        v = _along0(vhat)
+        assert v.shape[0] == self.M, "{} {}".format(v.shape[0], self.M)
+        return linear(v, lambda x: self._stencil_op(x, "pgx_stencil_to_chebyshev", self.N),
+                      lambda g: self._stencil_op(g, "pgx_stencil_transpose", self.M))
+
     def from_chebyshev(self, uhat):
-        """v = (S^T S)^-1 S^T u (chebyshev.py:295-337)."""
+        """v = (S^T S)^-1 S^T u (chebyshev.py:295-337); transpose S (S^T S)^-1."""
         u = _along0(uhat)
         assert u.shape[0] == self.N, "Shape mismatch ({:3}) ({:3})".format(u.shape[0], self.N)
-        out = empty_like_axis(u, 0, self.M)
-        p, s0, s1, _, nl = geom(u, 0)
-        q, t0, t1, _, _ = geom(out, 0)
-        _lib.check(_lib.lib().pgx_stencil_from_chebyshev(self._plan.h, p, s0, s1, q, t0, t1, nl, 0, stream()),
-                   "from_chebyshev")
-        return out
+        return linear(u, lambda x: self._stencil_op(x, "pgx_stencil_from_chebyshev", self.M),
+                      lambda g: self._stencil_op(g, "pgx_stencil_from_chebyshev_t", self.N))
 
     def eval_inhomogeneous(self, bchat):
         return self.bc.backward_fft(bchat)
@@ -312,11 +332,25 @@ class MatrixApply:
                                                       ctypes.byref(h)), "matrix plan")
         self.h = h
         self.banded = bool(_lib.lib().pgx_matrix_plan_is_banded(h))
+        self._A = A
+        self._T = None
+
+    @property
+    def T(self):
+        """The transposed operator (its own device plan, built on first use)."""
+        if self._T is None:
+            self._T = MatrixApply(self._A.T)
+            self._T._T = self
+        return self._T
 
     def apply(self, b, axis):
+        """out = A b along ``axis``; differentiable (transpose A^T)."""
         b = to_dev(b)
         if b.shape[axis] != self.cols:
             raise ValueError("Shape mismatch: N {:4d} | b.shape[axis] {:4d}".format(self.cols, b.shape[axis]))
+        return linear(b, lambda x: self._apply(x, axis), lambda g: self.T._apply(g, axis))
+
+    def _apply(self, b, axis):
         out = empty_like_axis(b, axis, self.rows)
         p, s0, s1, _, nl = geom(b, axis)
         q, t0, t1, _, _ = geom(out, axis)

@@ -71,9 +71,11 @@ static int check_program(const pgx_program* P) {
     if (op.a < 0 || op.a >= P->nslots) return PGX_E_ARG;
     const bool uses_b = op.code == PGX_OP_AXPY || op.code == PGX_OP_MUL || op.code == PGX_OP_COPY;
     if (uses_b && (op.b < 0 || op.b >= P->nslots)) return PGX_E_ARG;
-    const bool chain = op.code == PGX_OP_DIFF || op.code == PGX_OP_TDMA2 || op.code == PGX_OP_FDMA;
+    const bool chain = op.code == PGX_OP_DIFF || op.code == PGX_OP_DIFF_T || op.code == PGX_OP_TDMA2 ||
+                       op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T;
     if (chain && op.a + (op.b > 1 ? op.b : 1) > P->nslots) return PGX_E_ARG;
-    if (chain && op.code == PGX_OP_FDMA && op.mat + (op.b > 1 ? op.b : 1) > PGX_MAX_MAT) return PGX_E_ARG;
+    if (chain && (op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T) && op.mat + (op.b > 1 ? op.b : 1) > PGX_MAX_MAT)
+      return PGX_E_ARG;
     if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;
   }
   int64_t need = pgx_program_smem(P) + 1024;
@@ -113,6 +115,8 @@ static int check_instance(const pgx_program* P, const pgx_instance* I) {
       case PGX_OP_TDMA2:
       case PGX_OP_FDMA:
       case PGX_OP_POISSON:
+      case PGX_OP_FDMA_T:
+      case PGX_OP_POISSON_T:
       case PGX_OP_DCT:
         if (op.mat < 0 || !I->mat[op.mat]) return PGX_E_ARG;
         break;
@@ -217,10 +221,32 @@ int twiddles(int n, const double** out) {
   return PGX_OK;
 }
 
+// Host copies of the per-mode diagonal scalings of the kernels (y = post C (pre x)).
+double dct_pre_h(int mode, int j, int N) {
+  const bool end = (j == 0 || j == N);
+  const double sg = (j & 1) ? -1.0 : 1.0;
+  switch (mode) {
+    case PGX_DCT_BWD: return end ? sg : 0.5 * sg;
+    case PGX_DCT_FWD_T: return sg * (0.5 / N);
+    case PGX_DCT_BWD_T: return end ? 1.0 : 0.5;
+    default: return 1.0;
+  }
+}
+double dct_post_h(int mode, int k, int N) {
+  const bool end = (k == 0 || k == N);
+  const double sg = (k & 1) ? -1.0 : 1.0;
+  switch (mode) {
+    case PGX_DCT_FWD: return sg * (end ? 0.5 / N : 1.0 / N);
+    case PGX_DCT_FWD_T: return end ? 1.0 : 2.0;
+    case PGX_DCT_BWD_T: return sg;
+    default: return 1.0;
+  }
+}
+
 // DCT-I as a dense matrix with the Chebyshev pre/post scaling folded in.
 int dense_dct(int n, int mode, const double** out) {
   std::lock_guard<std::mutex> lk(g_mu);
-  auto key = std::make_pair(device_id(), n * 4 + mode);
+  auto key = std::make_pair(device_id(), n * 8 + mode);
   auto it = g_dense.find(key);
   if (it != g_dense.end()) {
     *out = it->second;
@@ -238,14 +264,7 @@ int dense_dct(int n, int mode, const double** out) {
         long long r = ((long long)j * k) % (2 * N);  // cos(pi j k / N) with exact argument reduction
         c = 2.0 * cos(pi * (double)r / (double)N);
       }
-      if (mode == PGX_DCT_BWD) {
-        double s = (j == 0 || j == N) ? 1.0 : 0.5;
-        c *= (j & 1) ? -s : s;
-      } else if (mode == PGX_DCT_FWD) {
-        double s = (k == 0 || k == N) ? 0.5 / N : 1.0 / N;
-        c *= (k & 1) ? -s : s;
-      }
-      h[(size_t)k * n + j] = c;
+      h[(size_t)k * n + j] = dct_post_h(mode, k, N) * c * dct_pre_h(mode, j, N);
     }
   double* d = nullptr;
   int rc = upload(h, &d);
@@ -345,7 +364,7 @@ extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t 
                         int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
                         void* stream) {
   if (!in || !out || n < 2 || n > PGX_LMAX - 8 || n_in < 0 || n_in > n || n_out < 0 || n_out > n || nlines < 0 ||
-      axis < 0 || axis > 1 || mode < 0 || mode > 2)
+      axis < 0 || axis > 1 || mode < 0 || mode > 4)
     return PGX_E_ARG;
   const double* tab = nullptr;
   bool fft = fft_length_ok(2 * (n - 1));
@@ -375,8 +394,21 @@ extern "C" int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in
 }
 
 // ------------------------------------------------------- derivative recurrence
+static int cheb_diff_op(int code, const double* c, int64_t c_s0, int64_t c_s1, double* dc, int64_t dc_s0,
+                        int64_t dc_s1, int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream);
+
 extern "C" int pgx_cheb_diff(const double* c, int64_t c_s0, int64_t c_s1, double* dc, int64_t dc_s0, int64_t dc_s1,
                              int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream) {
+  return cheb_diff_op(PGX_OP_DIFF, c, c_s0, c_s1, dc, dc_s0, dc_s1, n, nlines, axis, count, stream);
+}
+
+extern "C" int pgx_cheb_diff_t(const double* c, int64_t c_s0, int64_t c_s1, double* dc, int64_t dc_s0, int64_t dc_s1,
+                               int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream) {
+  return cheb_diff_op(PGX_OP_DIFF_T, c, c_s0, c_s1, dc, dc_s0, dc_s1, n, nlines, axis, count, stream);
+}
+
+static int cheb_diff_op(int code, const double* c, int64_t c_s0, int64_t c_s1, double* dc, int64_t dc_s0,
+                        int64_t dc_s1, int32_t n, int32_t nlines, int32_t axis, int32_t count, void* stream) {
   if (!c || !dc || n < 3 || n > PGX_LMAX - 8 || nlines < 0 || axis < 0 || axis > 1 || count < 0) return PGX_E_ARG;
   pgx_program P;
   pgx_instance I;
@@ -387,7 +419,7 @@ extern "C" int pgx_cheb_diff(const double* c, int64_t c_s0, int64_t c_s1, double
   set_axis_arr(I, 1, dc, dc_s0, dc_s1, axis, n, nlines);
   P.nops = 3;
   P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
-  P.ops[1] = mk(PGX_OP_DIFF, 0, -1, -1, -1, -1, count);
+  P.ops[1] = mk(code, 0, -1, -1, -1, -1, count);
   P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
   pick_tile(&P, nlines, n, 2, 0);
   return pgx_run(&P, &I, stream);
@@ -503,6 +535,52 @@ extern "C" int pgx_stencil_from_chebyshev(const pgx_stencil_plan* p, const doubl
   return pgx_run(&P, &I, stream);
 }
 
+// Transposes of the two stencil maps (adjoints for reverse mode):
+//   S^T: N -> N-2 points;  S (S^T S)^-1 (the transpose of from_chebyshev): N-2 -> N points.
+extern "C" int pgx_stencil_transpose(const pgx_stencil_plan* p, const double* in, int64_t in_s0, int64_t in_s1,
+                                     double* out, int64_t out_s0, int64_t out_s1, int32_t nlines, int32_t axis,
+                                     void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!in || !out || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->N;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, p->N, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, p->N - 2, nlines);
+  I.mat[0] = p->sub;
+  P.nops = 3;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_STENCIL_T, 0, -1, -1, 0);
+  P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->N, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
+extern "C" int pgx_stencil_from_chebyshev_t(const pgx_stencil_plan* p, const double* in, int64_t in_s0,
+                                            int64_t in_s1, double* out, int64_t out_s0, int64_t out_s1,
+                                            int32_t nlines, int32_t axis, void* stream) {
+  if (!p) return PGX_E_PLAN;
+  if (!in || !out || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
+  pgx_program P;
+  pgx_instance I;
+  init_prog(P, I, axis);
+  I.len[0] = nlines;
+  I.len[1] = p->N - 2;
+  set_axis_arr(I, 0, in, in_s0, in_s1, axis, p->N - 2, nlines);
+  set_axis_arr(I, 1, out, out_s0, out_s1, axis, p->N, nlines);
+  I.mat[0] = p->sub;
+  I.mat[1] = p->tdma;
+  P.nops = 4;
+  P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  P.ops[1] = mk(PGX_OP_TDMA2, 0, -1, -1, 1);
+  P.ops[2] = mk(PGX_OP_STENCIL, 0, -1, -1, 0);
+  P.ops[3] = mk(PGX_OP_STORE, 0, -1, 1);
+  pick_tile(&P, nlines, p->N, 2, 0);
+  return pgx_run(&P, &I, stream);
+}
+
 extern "C" int pgx_tdma_plan_create(const double* a, const double* b, const double* c, int32_t n, int32_t k,
                                     pgx_tdma_plan** plan) {
   if (!a || !b || !c || !plan || n < 3 || n > PGX_LMAX - 8 || k != 2) return PGX_E_ARG;
@@ -592,8 +670,21 @@ extern "C" int pgx_fdma_plan_destroy(pgx_fdma_plan* p) {
   return PGX_OK;
 }
 
+static int fdma_solve_op(int code, const pgx_fdma_plan* p, double* x, int64_t s0, int64_t s1, int32_t nlines,
+                         int32_t axis, void* stream);
+
 extern "C" int pgx_fdma_solve(const pgx_fdma_plan* p, double* x, int64_t s0, int64_t s1, int32_t nlines, int32_t axis,
                               void* stream) {
+  return fdma_solve_op(PGX_OP_FDMA, p, x, s0, s1, nlines, axis, stream);
+}
+
+extern "C" int pgx_fdma_solve_t(const pgx_fdma_plan* p, double* x, int64_t s0, int64_t s1, int32_t nlines,
+                                int32_t axis, void* stream) {
+  return fdma_solve_op(PGX_OP_FDMA_T, p, x, s0, s1, nlines, axis, stream);
+}
+
+static int fdma_solve_op(int code, const pgx_fdma_plan* p, double* x, int64_t s0, int64_t s1, int32_t nlines,
+                         int32_t axis, void* stream) {
   if (!p) return PGX_E_PLAN;
   if (!x || nlines < 0 || axis < 0 || axis > 1) return PGX_E_ARG;
   pgx_program P;
@@ -605,7 +696,7 @@ extern "C" int pgx_fdma_solve(const pgx_fdma_plan* p, double* x, int64_t s0, int
   I.mat[0] = p->tab;
   P.nops = 3;
   P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
-  P.ops[1] = mk(PGX_OP_FDMA, 0, -1, -1, 0);
+  P.ops[1] = mk(code, 0, -1, -1, 0);
   P.ops[2] = mk(PGX_OP_STORE, 0, -1, 0);
   pick_tile(&P, nlines, p->n, 2, 0);
   return pgx_run(&P, &I, stream);
@@ -679,8 +770,21 @@ extern "C" int pgx_poisson_plan_destroy(pgx_poisson_plan* p) {
   return PGX_OK;
 }
 
+static int poisson_solve_op(int code, const pgx_poisson_plan* p, double* x, int64_t s0, int64_t s1, int32_t axis,
+                            void* stream);
+
 extern "C" int pgx_poisson_solve(const pgx_poisson_plan* p, double* x, int64_t s0, int64_t s1, int32_t axis,
                                  void* stream) {
+  return poisson_solve_op(PGX_OP_POISSON, p, x, s0, s1, axis, stream);
+}
+
+extern "C" int pgx_poisson_solve_t(const pgx_poisson_plan* p, double* x, int64_t s0, int64_t s1, int32_t axis,
+                                   void* stream) {
+  return poisson_solve_op(PGX_OP_POISSON_T, p, x, s0, s1, axis, stream);
+}
+
+static int poisson_solve_op(int code, const pgx_poisson_plan* p, double* x, int64_t s0, int64_t s1, int32_t axis,
+                            void* stream) {
   if (!p) return PGX_E_PLAN;
   if (!x || axis < 0 || axis > 1) return PGX_E_ARG;
   pgx_program P;
@@ -692,7 +796,7 @@ extern "C" int pgx_poisson_solve(const pgx_poisson_plan* p, double* x, int64_t s
   I.mat[0] = p->tab;
   P.nops = 3;
   P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
-  P.ops[1] = mk(PGX_OP_POISSON, 0, -1, -1, 0);
+  P.ops[1] = mk(code, 0, -1, -1, 0);
   P.ops[2] = mk(PGX_OP_STORE, 0, -1, 0);
   pick_tile(&P, p->m, p->n, 2, 0);
   return pgx_run(&P, &I, stream);

@@ -313,6 +313,46 @@ __device__ void op_diff(Ctx& c, const pgx_op& op) {
   }
 }
 
+// Transpose of the derivative recurrence (adjoint of op_diff), in place:
+//   (D^T y)_i = 2i sum_{1 <= j < i, j = i+1 mod 2} y_j + y_0 [i odd] (1 if i = 1 else i).
+// Warp-parallel forward prefix sums per parity class.
+__device__ void op_diff_t(Ctx& c, const pgx_op& op) {
+  const int ns = nslot_of(op);
+  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+  for (int w = warp; w < ns * c.tb; w += nw) {
+    const int s = w / c.tb, t = w - s * c.tb;
+    const int n = c.slen[op.a + s];
+    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    const int chunk = (n + 31) >> 5;
+    const int a = lane * chunk, b = min(a + chunk, n);
+    for (int rep = 0; rep < op.k; ++rep) {
+      double tot[2] = {0.0, 0.0};
+      for (int i = max(a, 1); i < b; ++i) tot[i & 1] += x[i];
+      const double y0 = x[0];
+      double in0 = tot[0], in1 = tot[1];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double v0 = __shfl_up_sync(0xffffffffu, in0, o);
+        const double v1 = __shfl_up_sync(0xffffffffu, in1, o);
+        if (lane >= o) {
+          in0 += v0;
+          in1 += v1;
+        }
+      }
+      double acc[2] = {in0 - tot[0], in1 - tot[1]};  // sums over j < a, j >= 1
+      __syncwarp();
+      for (int i = a; i < b; ++i) {
+        const double yi = x[i];
+        double v = c_twok.v[i] * acc[(i + 1) & 1];
+        if (i & 1) v = fma(i == 1 ? 1.0 : 0.5 * c_twok.v[i], y0, v);
+        x[i] = v;
+        if (i >= 1) acc[i & 1] += yi;
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // In-place banded LU sweep for offsets -2, 0, +2, +4 (fdma.f90:1-38) with
 // factors [l | dinv | u1 | u2] (each n, zero-padded, l[i] couples x_i to x_{i-2}):
 //   forward  x_i -= l_i x_{i-2};   backward x_i = (x_i - u1_i x_{i+2} - u2_i x_{i+4}) dinv_i
@@ -339,7 +379,34 @@ __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, 
 
 // FDMA over ns slots: slot a+s uses factor table mat+s.  POISSON (per_line):
 // single table with per-line factors.
-__device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line) {
+// Transposed solve A^T x = b with the factors of A = L U (adjoint of fdma_chain):
+//   U^T z = b (forward):  z_i = (b_i - u1_{i-2} z_{i-2} - u2_{i-4} z_{i-4}) dinv_i
+//   L^T x = z (backward): x_i = z_i - l_{i+2} x_{i+2}
+__device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n, int p) {
+  const double* l = tab;
+  const double* dinv = tab + n;
+  const double* u1 = tab + 2 * n;
+  const double* u2 = tab + 3 * n;
+  double z2 = 0.0, z4 = 0.0;
+  int i = p;
+  for (; i < n; i += 2) {
+    double v = x[i];
+    if (i >= 4) v = fma(-__ldg(u2 + i - 4), z4, v);
+    if (i >= 2) v = fma(-__ldg(u1 + i - 2), z2, v);
+    v *= __ldg(dinv + i);
+    x[i] = v;
+    z4 = z2;
+    z2 = v;
+  }
+  double xn = 0.0;
+  for (i -= 2; i >= 0; i -= 2) {
+    const double li = (i + 2 < n) ? __ldg(l + i + 2) : 0.0;
+    xn = fma(-li, xn, x[i]);
+    x[i] = xn;
+  }
+}
+
+__device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line, bool transpose = false) {
   int s, t, p;
   const int ns = nslot_of(op);
   for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
@@ -351,7 +418,8 @@ __device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool pe
     if (p >= n || line >= c.nlines) continue;
     const double* tab = I.mat[op.mat + (per_line ? 0 : s)];
     if (per_line) tab += (size_t)line * 4 * n;
-    fdma_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
+    if (transpose) fdma_t_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
+    else fdma_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
   }
 }
 
@@ -417,6 +485,38 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
+// Diagonal scalings around the raw DCT-I matrix C (y = post * C (pre * x)), per mode:
+//   RAW 1, 1;  FWD 1, m_k (-1)^k / (2N);  BWD (-1)^j / w_j, 1;
+//   FWD_T (-1)^j / (2N), w_k;  BWD_T 1 / w_j, (-1)^k   (w = 1 at both ends, 2 inside;
+// the transposed modes are the exact adjoints of FWD and BWD because C^T = W C W^-1).
+// Every pre-scale is symmetric in j <-> N - j for even N.
+__device__ __forceinline__ double dct_pre(int mode, int j, int N) {
+  const bool end = (j == 0 || j == N);
+  const double sg = (j & 1) ? -1.0 : 1.0;
+  switch (mode) {
+    case PGX_DCT_BWD: return end ? sg : 0.5 * sg;
+    case PGX_DCT_FWD_T: return sg * (0.5 / N);
+    case PGX_DCT_BWD_T: return end ? 1.0 : 0.5;
+    default: return 1.0;
+  }
+}
+__device__ __forceinline__ double dct_post(int mode, int k, int N) {
+  const bool end = (k == 0 || k == N);
+  const double sg = (k & 1) ? -1.0 : 1.0;
+  switch (mode) {
+    case PGX_DCT_FWD: return sg * (end ? 0.5 / N : 1.0 / N);
+    case PGX_DCT_FWD_T: return end ? 1.0 : 2.0;
+    case PGX_DCT_BWD_T: return sg;
+    default: return 1.0;
+  }
+}
+__device__ __forceinline__ bool dct_has_pre(int mode) {
+  return mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
+}
+__device__ __forceinline__ bool dct_has_post(int mode) {
+  return mode == PGX_DCT_FWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
+}
+
 // One radix-R Stockham stage over `npairs` pairs of lines.
 //   FIRST: the input is the even extension of slot lines (2p, 2p+1), read straight
 //          from the slot with the backward pre-scale folded in (no copy pass);
@@ -428,7 +528,6 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
   const int LR = L / R;
   const int step = tws * (L / (Ns * R));  // twiddle table holds exp(-2 pi i k / (tws L))
   const int N = L >> 1;
-  const double invN = 1.0 / N;
   for (int idx = c.tid; idx < npairs * LR; idx += c.nthreads) {
     int pr = idx / LR, j = idx - pr * LR;
     const int t0 = 2 * pr;
@@ -442,10 +541,8 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
         const int sidx = m <= N ? m : L - m;
         double a = x[t0 * c.lcap + sidx];
         double b = two ? x[(t0 + 1) * c.lcap + sidx] : 0.0;
-        if (mode == PGX_DCT_BWD) {
-          // g_s = (-1)^s c_s, doubled at both ends, times the final 1/2
-          double w = (sidx == 0 || sidx == N) ? 1.0 : 0.5;
-          if (sidx & 1) w = -w;
+        if (dct_has_pre(mode)) {
+          const double w = dct_pre(mode, sidx, N);
           a *= w;
           b *= w;
         }
@@ -485,10 +582,8 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
       if (LAST) {
         if (kk <= N) {
           double2 z = o[q];
-          if (mode == PGX_DCT_FWD) {
-            // c_k = m_k (-1)^k y_k / (2N)
-            double sc = (kk == 0 || kk == N) ? 0.5 * invN : invN;
-            if (kk & 1) sc = -sc;
+          if (dct_has_post(mode)) {
+            const double sc = dct_post(mode, kk, N);
             z.x *= sc;
             z.y *= sc;
           }
@@ -535,15 +630,13 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, op.a);
   const int npairs = (c.tb + 1) >> 1;
-  const double invN = 1.0 / N;
   // fold
   for (int idx = c.tid; idx < npairs * N; idx += c.nthreads) {
     const int pr = idx / N, j = idx - pr * N;
     const int t0 = 2 * pr;
     const bool two = t0 + 1 < c.tb;
     const double sn = -__ldg(&tw[j].y);
-    double sg = 1.0;
-    if (mode == PGX_DCT_BWD && j > 0) sg = (j & 1) ? -0.5 : 0.5;
+    const double sg = dct_has_pre(mode) ? dct_pre(mode, j, N) : 1.0;
     const double a0 = x[t0 * c.lcap + j], a1 = x[t0 * c.lcap + N - j];
     double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
     double ub = 0.0;
@@ -551,7 +644,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       const double b0 = x[(t0 + 1) * c.lcap + j], b1 = x[(t0 + 1) * c.lcap + N - j];
       ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
     }
-    if (mode == PGX_DCT_BWD) {
+    if (dct_has_pre(mode)) {
       ua *= sg;
       ub *= sg;
     }
@@ -565,12 +658,13 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       double acc = 0.0;
       for (int j = 1 + lane; j < H; j += 32) {
         double d = xl[j] - xl[N - j];
-        if (mode == PGX_DCT_BWD) d *= (j & 1) ? -0.5 : 0.5;
+        if (dct_has_pre(mode)) d *= dct_pre(mode, j, N);
         acc = fma(__ldg(&tw[j].x), d, acc);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) c.ybuf[t] = fma(2.0, acc, xl[0] - xl[N]);
+      const double d0 = (xl[0] - xl[N]) * (dct_has_pre(mode) ? dct_pre(mode, 0, N) : 1.0);
+      if (lane == 0) c.ybuf[t] = fma(2.0, acc, d0);
     }
   }
   __syncthreads();
@@ -594,8 +688,8 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     const double2 zm = Z[pr * c.fft_stride + m];
     const double2 zn = Z[pr * c.fft_stride + (m == 0 ? 0 : N - m)];
     double ya = zm.x + zn.x, yb = zm.y + zn.y;
-    if (mode == PGX_DCT_FWD) {
-      const double sc = (m == 0 || m == H) ? 0.5 * invN : invN;  // (-1)^{2m} = 1
+    if (dct_has_post(mode)) {
+      const double sc = dct_post(mode, 2 * m, N);
       ya *= sc;
       yb *= sc;
     }
@@ -614,7 +708,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
     const int chunk = (H + 31) / 32;
-    const double osc = mode == PGX_DCT_FWD ? -invN : 1.0;  // odd k: (-1)^k / N
+    const double osc = dct_has_post(mode) ? dct_post(mode, 1, N) : 1.0;  // the same for every odd k < N
     for (int t = warp; t < c.tb; t += nw) {
       double* xl = x + t * c.lcap;
       const int m0 = lane * chunk, m1 = min(m0 + chunk, H);
@@ -682,15 +776,11 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     __syncthreads();
   }
   if (nst == 1) {  // tiny transform: copy the single stage's output back
-    const double invN = 1.0 / N;
     for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
       int t = idx / n, k = idx - t * n;
       double2 z = c.f0[(t >> 1) * c.fft_stride + k];
       double y = (t & 1) ? z.y : z.x;
-      if (mode == PGX_DCT_FWD) {
-        double sc = (k == 0 || k == N) ? 0.5 * invN : invN;
-        y *= (k & 1) ? -sc : sc;
-      }
+      if (dct_has_post(mode)) y *= dct_post(mode, k, N);
       x[t * c.lcap + k] = y;
     }
   }
@@ -744,6 +834,9 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
       case PGX_OP_DENSE: op_dense(c, op, I); break;
       case PGX_OP_FDMA: op_fdma(c, op, I, false); break;
       case PGX_OP_POISSON: op_fdma(c, op, I, true); break;
+      case PGX_OP_DIFF_T: op_diff_t(c, op); break;
+      case PGX_OP_FDMA_T: op_fdma(c, op, I, false, true); break;
+      case PGX_OP_POISSON_T: op_fdma(c, op, I, true, true); break;
       case PGX_OP_ZERO00:
         if (c.l0 == 0 && c.tid == 0) slot_ptr(c, op.a)[0] = 0.0;
         break;

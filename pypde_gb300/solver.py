@@ -12,6 +12,7 @@ import scipy.sparse as sp
 
 from . import _lib
 from ._dev import geom, stream, to_dev
+from .autodiff import linear, recording
 from .bases import MatrixApply
 from .host import fdma_lu
 
@@ -113,13 +114,21 @@ class Plan_numpy(MetaPlan):
 
 
 class _InPlaceBanded(MetaPlan):
-    def _solve_inplace(self, b):
-        b = to_dev(b)
-        self._check_b(b)
+    def _sweep(self, b, fn):
         axis = self.axis if b.dim() == 2 else 0
         p, s0, s1, _, nl = geom(b, axis)
-        _lib.check(_lib.lib().pgx_fdma_solve(self._h, p, s0, s1, nl, axis, stream()), self.flags["method"])
+        _lib.check(getattr(_lib.lib(), fn)(self._h, p, s0, s1, nl, axis, stream()), self.flags["method"])
         return b
+
+    def _solve_inplace(self, b):
+        """In place, like the Fortran intent(inout).  While autograd records, the solve
+        is out of place and its backward is the transposed solve A^T x = g."""
+        b = to_dev(b)
+        self._check_b(b)
+        if recording(b):
+            return linear(b, lambda x: self._sweep(x.clone(), "pgx_fdma_solve"),
+                          lambda g: self._sweep(g.clone(), "pgx_fdma_solve_t"))
+        return self._sweep(b, "pgx_fdma_solve")
 
     def __del__(self):
         try:
@@ -194,8 +203,14 @@ class Plan_Poisson(MetaPlan):
         if self.alpha.size != b.shape[1 - self.axis]:
             raise ValueError("Size of eigenvalue {:3} array does not match to b {:3}!".format(
                 self.alpha.size, b.shape[1 - self.axis]))
+        if recording(b):
+            return linear(b, lambda x: self._sweep(x.clone(), "pgx_poisson_solve"),
+                          lambda g: self._sweep(g.clone(), "pgx_poisson_solve_t"))
+        return self._sweep(b, "pgx_poisson_solve")
+
+    def _sweep(self, b, fn):
         p, s0, s1, _, _ = geom(b, self.axis)
-        _lib.check(_lib.lib().pgx_poisson_solve(self._h, p, s0, s1, self.axis, stream()), "poisson")
+        _lib.check(getattr(_lib.lib(), fn)(self._h, p, s0, s1, self.axis, stream()), "poisson")
         return b
 
     def __del__(self):
