@@ -26,13 +26,14 @@ class LinearMap(torch.autograd.Function):
     """y = A x for a device linear operator A, with x_bar = A^T y_bar in backward."""
 
     @staticmethod
-    def forward(ctx, x, apply, apply_t):
-        ctx.apply, ctx.apply_t = apply, apply_t
-        return apply(x)
+    def forward(ctx, x, op, op_t):
+        # (not ctx.apply: that name is the autograd node's own entry point)
+        ctx.op, ctx.op_t = op, op_t
+        return op(x)
 
     @staticmethod
     def backward(ctx, g):
-        return linear(_sane(g), ctx.apply_t, ctx.apply), None, None
+        return linear(_sane(g), ctx.op_t, ctx.op), None, None
 
 
 def recording(x):

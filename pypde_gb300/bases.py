@@ -225,7 +225,9 @@ class GalerkinChebyshev(MetaBase):
             u = u + self.bc.to_chebyshev(bc)
         return self.family.backward_fft(u)
 
-    def _stencil_op(self, x, fn, n_out):
+    def _stencil_op(self, x, fn, n_in, n_out):
+        if x.shape[0] != n_in:
+            raise ValueError("%s: expected %d points along the axis, got %d" % (fn, n_in, x.shape[0]))
         out = empty_like_axis(x, 0, n_out)
         p, s0, s1, _, nl = geom(x, 0)
         q, t0, t1, _, _ = geom(out, 0)
@@ -236,15 +238,15 @@ class GalerkinChebyshev(MetaBase):
         """u = S v (chebyshev.py:287-293); transpose S^T."""
         v = _along0(vhat)
         assert v.shape[0] == self.M, "{} {}".format(v.shape[0], self.M)
-        return linear(v, lambda x: self._stencil_op(x, "pgx_stencil_to_chebyshev", self.N),
-                      lambda g: self._stencil_op(g, "pgx_stencil_transpose", self.M))
+        return linear(v, lambda x: self._stencil_op(x, "pgx_stencil_to_chebyshev", self.M, self.N),
+                      lambda g: self._stencil_op(g, "pgx_stencil_transpose", self.N, self.M))
 
     def from_chebyshev(self, uhat):
         """v = (S^T S)^-1 S^T u (chebyshev.py:295-337); transpose S (S^T S)^-1."""
         u = _along0(uhat)
         assert u.shape[0] == self.N, "Shape mismatch ({:3}) ({:3})".format(u.shape[0], self.N)
-        return linear(u, lambda x: self._stencil_op(x, "pgx_stencil_from_chebyshev", self.M),
-                      lambda g: self._stencil_op(g, "pgx_stencil_from_chebyshev_t", self.N))
+        return linear(u, lambda x: self._stencil_op(x, "pgx_stencil_from_chebyshev", self.N, self.M),
+                      lambda g: self._stencil_op(g, "pgx_stencil_from_chebyshev_t", self.M, self.N))
 
     def eval_inhomogeneous(self, bchat):
         return self.bc.backward_fft(bchat)
@@ -351,6 +353,8 @@ class MatrixApply:
         return linear(b, lambda x: self._apply(x, axis), lambda g: self.T._apply(g, axis))
 
     def _apply(self, b, axis):
+        if b.shape[axis] != self.cols:
+            raise ValueError("Shape mismatch: N {:4d} | b.shape[axis] {:4d}".format(self.cols, b.shape[axis]))
         out = empty_like_axis(b, axis, self.rows)
         p, s0, s1, _, nl = geom(b, axis)
         q, t0, t1, _, _ = geom(out, axis)

@@ -106,12 +106,15 @@ class Prog:
     def setlen(self, s, n):
         self.add("SETLEN", s, len=n)
 
+    _DENSE_DCT = {_lib.DCT_FWD: "dct_fwd", _lib.DCT_BWD: "dct_bwd", _lib.DCT_FWD_T: "dct_fwd_t",
+                  _lib.DCT_BWD_T: "dct_bwd_t"}
+
     def dct(self, s, mode, fft):
         self.has_dct = True
         if fft:
             self.add("DCT", s, mat="dct", k=mode)
         else:
-            self.add("DENSE", s, mat="dct_fwd" if mode == _lib.DCT_FWD else "dct_bwd", len=L_ND + self.axis)
+            self.add("DENSE", s, mat=self._DENSE_DCT[mode], len=L_ND + self.axis)
 
     def banded(self, s, name, off0, ndiag, rows):
         self.add("BANDED", s, b=off0, mat=name, len=rows, k=ndiag)
@@ -119,8 +122,9 @@ class Prog:
     def dense(self, s, name, rows):
         self.add("DENSE", s, mat=name, len=rows)
 
-    def fdma(self, s, names):
-        """One FDMA op over consecutive slots s, s+1, ... with factor tables ``names``."""
+    def fdma(self, s, names, code="FDMA"):
+        """One FDMA op over consecutive slots s, s+1, ... with factor tables ``names``
+        (``code`` FDMA_T: the transposed solve with the same factors)."""
         if isinstance(names, str):
             names = [names]
         first = None
@@ -129,7 +133,16 @@ class Prog:
             idx = self._m(key)
             first = idx if first is None else first
             assert idx == first + i
-        self.ops.append(_lib.op("FDMA", a=s, b=len(names), mat=first))
+        self.ops.append(_lib.op(code, a=s, b=len(names), mat=first))
+
+    def fdma_t(self, s, names):
+        self.fdma(s, names, code="FDMA_T")
+
+    def diff_t(self, s, count=1):
+        self.add("DIFF_T", s, k=count)
+
+    def store_add(self, s, arr, alpha=1.0, par=-1):
+        self.add("STORE_ADD", s, arr=arr, alpha=alpha, par=par)
 
     def tdma_multi(self, s, count, kind):
         self.add("TDMA2", s, b=count, mat="tdma_" + kind)
@@ -329,21 +342,18 @@ def build_programs(tkind, fft):
 _GLOBAL = {}
 
 
-def _global_tables():
-    """Length-independent device tables: stencil sub-diagonals and offset-2 TDMA factors.
+def global_tables_host():
+    """Length-independent tables: stencil sub-diagonals and offset-2 TDMA factors.
 
     For the Shen CD / CN stencils S[i+2, i] depends on i only, and so do the
     forward factors of the TDMA on S^T S (the last two w_i of a shorter system
     are never used by the sweep), so one long table serves every size.
     """
-    dev = torch.cuda.current_device()
-    if dev in _GLOBAL:
-        return _GLOBAL[dev]
     n = _lib.LMAX - 8
     t = {}
     for kind in ("CD", "CN"):
         sub = stencil_sub(kind, n + 2)
-        t["sten_" + kind] = to_dev(np.concatenate([sub, np.zeros(2)]))
+        t["sten_" + kind] = np.concatenate([sub, np.zeros(2)])
         b = 1.0 + sub * sub
         a = sub.copy()
         c = sub.copy()
@@ -355,9 +365,16 @@ def _global_tables():
             w[i] = c[i] / den
             rden[i] = 1.0 / den
             aa[i] = 0.0 if i < 2 else a[i - 2]
-        t["tdma_" + kind] = (n, to_dev(np.stack([aa, rden, w], axis=1).ravel()))
-    _GLOBAL[dev] = t
+        t["tdma_" + kind] = np.stack([aa, rden, w], axis=1).ravel()
     return t
+
+
+def _global_tables():
+    """global_tables_host() on the current device (built once per device)."""
+    dev = torch.cuda.current_device()
+    if dev not in _GLOBAL:
+        _GLOBAL[dev] = {k: to_dev(v) for k, v in global_tables_host().items()}
+    return _GLOBAL[dev]
 
 
 def _banded_table(A, off0, ndiag):
@@ -376,7 +393,7 @@ def _banded_table(A, off0, ndiag):
             if 0 <= c < cols:
                 R[r, c] = tab[d, r]
     assert np.array_equal(R, A), "matrix is not banded on the expected diagonals"
-    return to_dev(tab.ravel())
+    return tab.ravel()
 
 
 def _fdma_table(A):
@@ -387,7 +404,7 @@ def _fdma_table(A):
     tab[1] = 1.0 / d
     tab[2, :n - 2] = u1
     tab[3, :n - 4] = u2
-    return to_dev(tab.ravel())
+    return tab.ravel()
 
 
 def _poisson_table(Ax, Cx, lam):
@@ -405,14 +422,11 @@ def _poisson_table(Ax, Cx, lam):
         tab[j, 1, o:] = 1.0 / d
         tab[j, 2, o:o + ns - 2] = u1
         tab[j, 3, o:o + ns - 4] = u2
-    return to_dev(tab.ravel())
+    return tab.ravel()
 
 
-def _dct_tables(n, fft):
-    if fft:
-        h = ctypes.c_void_p()
-        _lib.check(_lib.lib().pgx_dct_table(n, ctypes.byref(h)), "dct table")
-        return {"dct": h.value}
+def dense_dct_host(n):
+    """Dense DCT matrices (n x n, row-major) with the Chebyshev scalings folded in, and their transposes."""
     N = n - 1
     k = np.arange(n)[:, None]
     j = np.arange(n)[None, :]
@@ -421,7 +435,81 @@ def _dct_tables(n, fft):
     C[:, -1] = (-1.0) ** np.arange(n)
     pre = np.where((j == 0) | (j == N), 1.0, 0.5) * (-1.0) ** j
     post = np.where((k == 0) | (k == N), 0.5 / N, 1.0 / N) * (-1.0) ** k
-    return {"dct_bwd": to_dev(C * pre), "dct_fwd": to_dev(C * post)}
+    bwd, fwd = C * pre, C * post
+    return {"dct_bwd": bwd, "dct_fwd": fwd, "dct_bwd_t": np.ascontiguousarray(bwd.T),
+            "dct_fwd_t": np.ascontiguousarray(fwd.T)}
+
+
+def _dct_tables(n, fft):
+    if fft:
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().pgx_dct_table(n, ctypes.byref(h)), "dct table")
+        return {"dct": h.value}
+    return {k: to_dev(v) for k, v in dense_dct_host(n).items()}
+
+
+def host_tables(N, M, tk, dt, nu, kappa, scale, fd, adjoint=False):
+    """Operator tables of one instance (host, device layout): banded B / B S, the
+    pre-factored ADI sweeps, the Poisson per-eigenvalue factors, H_y, Q_y and, with
+    ``adjoint``, the transposed tables of the reverse-mode passes.  ``fd`` holds the
+    fast-diagonalisation matrices Ax, Cx, wy, Qy, Hy of the pressure plan."""
+    sx, sz = scale
+    t = {}
+    Bx, By = pseudoinverse_d2(N)[2:, :], pseudoinverse_d2(M)[2:, :]
+    Sx_U, Sx_T, Sy = stencil_matrix("CD", N), stencil_matrix(tk, N), stencil_matrix("CD", M)
+    t["Bx"] = _banded_table(Bx, 0, 3)
+    t["By"] = _banded_table(By, 0, 3)
+    t["BSx_U"] = _banded_table(Bx @ Sx_U, -2, 4)
+    t["BSx_T"] = _banded_table(Bx @ Sx_T, -2, 4)
+    t["BSy"] = _banded_table(By @ Sy, -2, 4)
+    Ix, Iy = np.eye(N)[2:, :], np.eye(M)[2:, :]
+    lu, lt = dt * nu, dt * kappa
+    t["Ax_U"] = _fdma_table(Bx @ Sx_U - lu / sx ** 2 * Ix @ Sx_U)
+    t["Ax_T"] = _fdma_table(Bx @ Sx_T - lt / sx ** 2 * Ix @ Sx_T)
+    t["Ay_U"] = _fdma_table(By @ Sy - lu / sz ** 2 * Iy @ Sy)
+    t["Ay_T"] = _fdma_table(By @ Sy - lt / sz ** 2 * Iy @ Sy)
+    t["Pois"] = _poisson_table(np.asarray(fd["Ax"]), np.asarray(fd["Cx"]), np.real(fd["wy"]))
+    Hy, Qy = np.real(np.asarray(fd["Hy"])), np.real(np.asarray(fd["Qy"]))
+    t["Hy"] = np.ascontiguousarray(Hy)
+    t["Qy"] = np.ascontiguousarray(Qy)
+    if adjoint:
+        T = lambda A: np.ascontiguousarray(A.T)  # noqa: E731
+        t["BxT"] = _banded_table(T(Bx), -4, 3)
+        t["ByT"] = _banded_table(T(By), -4, 3)
+        t["BSx_UT"] = _banded_table(T(Bx @ Sx_U), -4, 4)
+        t["BSx_TT"] = _banded_table(T(Bx @ Sx_T), -4, 4)
+        t["BSyT"] = _banded_table(T(By @ Sy), -4, 4)
+        t["HyT"] = T(Hy)
+        t["QyT"] = T(Qy)
+    return t
+
+
+def instance_params(N, M, dealias, dt, nu, kappa, scale):
+    """len[] and par[] of one instance (indices L_* and P_*)."""
+    Nd, Md = (int(1.5 * N), int(1.5 * M)) if dealias else (N, M)
+    sx, sz = scale
+    lens = [0, N, M, N - 2, M - 2, Nd, Md]
+    par = [1.0 / sx, 1.0 / sz, -dt, dt, dt * kappa, -dt / sx, -dt / sz, -nu, 1.0 / dt]
+    return lens, par
+
+
+def scratch_shapes(N, M, Nd, Md):
+    """Intermediate arrays of the forward passes (name -> shape)."""
+    sh = {}
+    for F in "UVT":
+        sh["A_" + F + "0"] = (Nd, M - 2)
+        sh["A_" + F + "x"] = (Nd, M - 2)
+        sh["C_" + F] = (Nd, M)
+        sh["RHS_" + F] = (N, M)
+        sh["Q1_" + F] = (N - 2, M)
+        sh["Q2_" + F] = (N - 2, M - 2)
+    sh["DPZ"] = (N, M)
+    sh["TSY"] = (N - 2, M)
+    for k in ("W1", "W2", "R1", "Y1", "Y2", "G1", "G2"):
+        sh[k] = (N - 2, M)
+    sh["R2"] = (N - 2, M - 2)
+    sh["X"] = (N - 2, M - 2)
+    return sh
 
 
 class _Instance:
@@ -455,45 +543,15 @@ class _Instance:
         a["TBCC"] = ns.Tbc_cheby.contiguous()
         a["DTB1"] = ns.dTbcdz1.contiguous()
         a["DTB2"] = ns.dTbcdz2.contiguous()
-        for F in "UVT":
-            a["A_" + F + "0"] = z(Nd, M - 2)
-            a["A_" + F + "x"] = z(Nd, M - 2)
-            a["C_" + F] = z(Nd, M)
-            a["RHS_" + F] = z(N, M)
-            a["Q1_" + F] = z(N - 2, M)
-            a["Q2_" + F] = z(N - 2, M - 2)
-        a["DPZ"] = z(N, M)
-        a["TSY"] = z(N - 2, M)
-        for k in ("W1", "W2", "R1", "Y1", "Y2", "G1", "G2"):
-            a[k] = z(N - 2, M)
-        a["R2"] = z(N - 2, M - 2)
-        a["X"] = z(N - 2, M - 2)
+        for k, shp in scratch_shapes(N, M, Nd, Md).items():
+            a[k] = z(*shp)
         self.arrays = a
-        self.lens = [0, N, M, N - 2, M - 2, Nd, Md]
-        sx, sz = ns.scale
-        dt, nu, kap = ns.dt, ns.nu, ns.kappa
-        self.par = [1.0 / sx, 1.0 / sz, -dt, dt, dt * kap, -dt / sx, -dt / sz, -nu, 1.0 / dt]
+        self.lens, self.par = instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale)
         # operator tables
         g = _global_tables()
-        t = {"sten_CD": g["sten_CD"], "sten_CN": g["sten_CN"], "tdma_CD": g["tdma_CD"][1]}
-        tk = ns.T.xs[0].id
-        Bx, By = pseudoinverse_d2(N)[2:, :], pseudoinverse_d2(M)[2:, :]
-        Sx_U, Sx_T, Sy = stencil_matrix("CD", N), stencil_matrix(tk, N), stencil_matrix("CD", M)
-        t["Bx"] = _banded_table(Bx, 0, 3)
-        t["By"] = _banded_table(By, 0, 3)
-        t["BSx_U"] = _banded_table(Bx @ Sx_U, -2, 4)
-        t["BSx_T"] = _banded_table(Bx @ Sx_T, -2, 4)
-        t["BSy"] = _banded_table(By @ Sy, -2, 4)
-        Ix, Iy = np.eye(N)[2:, :], np.eye(M)[2:, :]
-        lu, lt = dt * nu, dt * kap
-        t["Ax_U"] = _fdma_table(Bx @ Sx_U - lu / sx ** 2 * Ix @ Sx_U)
-        t["Ax_T"] = _fdma_table(Bx @ Sx_T - lt / sx ** 2 * Ix @ Sx_T)
-        t["Ay_U"] = _fdma_table(By @ Sy - lu / sz ** 2 * Iy @ Sy)
-        t["Ay_T"] = _fdma_table(By @ Sy - lt / sz ** 2 * Iy @ Sy)
-        fd = ns.solver_P._fd
-        t["Pois"] = _poisson_table(np.asarray(fd["Ax"]), np.asarray(fd["Cx"]), np.real(fd["wy"]))
-        t["Hy"] = to_dev(np.ascontiguousarray(np.real(fd["Hy"])))
-        t["Qy"] = to_dev(np.ascontiguousarray(np.real(fd["Qy"])))
+        t = {"sten_CD": g["sten_CD"], "sten_CN": g["sten_CN"], "tdma_CD": g["tdma_CD"]}
+        host = host_tables(N, M, ns.T.xs[0].id, ns.dt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
+        t.update({k: to_dev(v) for k, v in host.items()})
         self.tables = t
         self.dct_x = _dct_tables(Nd, fft)
         self.dct_y = _dct_tables(Md, fft)
@@ -548,7 +606,8 @@ def program_maxlen(prog, lens):
     return m
 
 
-CHAIN_OPS = ("FDMA", "POISSON", "TDMA2")
+CHAIN_OPS = ("FDMA", "POISSON", "TDMA2", "FDMA_T", "POISSON_T")
+_CHAIN_CODES = tuple(_lib.OP[k] for k in CHAIN_OPS)
 
 
 def fft_bytes_per_line(fft_n):
@@ -591,9 +650,9 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     # one thread per (slot, line, parity) chain of the widest chain op
     width = 1
     for o in prog.ops:
-        if o.code in (_lib.OP["FDMA"], _lib.OP["TDMA2"], _lib.OP["POISSON"]):
+        if o.code in _CHAIN_CODES:
             width = max(width, 2 * max(o.b, 1))
-        elif o.code == _lib.OP["DIFF"]:
+        elif o.code in (_lib.OP["DIFF"], _lib.OP["DIFF_T"]):
             width = max(width, max(o.b, 1))
     nt = max(256, 32 * -(-width * tb // 32))
     return tb, min(nt, 1024)
@@ -606,9 +665,9 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     per_line = 8 * nbuf * lcap + fft_bytes_per_line(fft_n)
     width = 1
     for o in prog.ops:
-        if o.code in (_lib.OP["FDMA"], _lib.OP["TDMA2"], _lib.OP["POISSON"]):
+        if o.code in _CHAIN_CODES:
             width = max(width, 2 * max(o.b, 1))
-        elif o.code == _lib.OP["DIFF"]:
+        elif o.code in (_lib.OP["DIFF"], _lib.OP["DIFF_T"]):
             width = max(width, max(o.b, 1))
     tbs = set()
     for ctas in (1, 2, 3, 4):
@@ -837,7 +896,7 @@ def program_work(prog, I):
             fl += 2.0 * slen[o.a] * lines
         elif code == _lib.OP["TDMA2"]:
             fl += 5.0 * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
-        elif code == _lib.OP["DIFF"]:
+        elif code in (_lib.OP["DIFF"], _lib.OP["DIFF_T"]):
             fl += 2.0 * o.k * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
         elif code == _lib.OP["DCT"]:
             n = slen[o.a]
@@ -849,9 +908,9 @@ def program_work(prog, I):
             cols = slen[o.a]
             slen[o.a] = I.lens[o.len]
             fl += 2.0 * cols * slen[o.a] * lines
-        elif code == _lib.OP["FDMA"]:
+        elif code in (_lib.OP["FDMA"], _lib.OP["FDMA_T"]):
             fl += 7.0 * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
-        elif code == _lib.OP["POISSON"]:
+        elif code in (_lib.OP["POISSON"], _lib.OP["POISSON_T"]):
             fl += 9.0 * slen[o.a] * lines
     return fl, by
 

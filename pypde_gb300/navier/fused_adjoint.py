@@ -1,0 +1,502 @@
+"""Reverse-mode (discrete adjoint) fused step: thirteen line-program passes.
+
+The forward fused step (``fused.build_programs``) maps the state
+(U, V, T Galerkin coefficients and the Chebyshev pressure) to the next one.
+Its adjoint maps the gradient with respect to the new state to the gradient
+with respect to the old state.  Every forward pass is linear in its inputs
+except the convection products of P2, so the adjoint is the forward pass
+sequence run backwards with every operator replaced by its transpose:
+
+  LOAD <-> STORE / STORE_ADD, S <-> S^T, D -> D^T (DIFF_T), DCT FWD/BWD ->
+  FWD_T/BWD_T, pad <-> truncate, banded / dense tables -> transposed tables,
+  FDMA -> FDMA_T, POISSON -> POISSON_T, the symmetric (S^T S)^-1 and the
+  projection P[0,0] = 0 unchanged.
+
+The products ux * dF/dx and uz * dF/dz are linearised around the forward state
+of the step: pass R1 (the forward P1) recomputes A_F0 / A_Fx from that state,
+and Q2a / Q2b recompute ux, uz and the physical derivatives inside the pass.
+
+  R1  x  forward P1 on the step's input state        -> A_F0, A_Fx
+  Q10 y  velocity correction^T                       -> U*bar, V*bar, G1bar, G2bar
+  Q9  x  pressure update^T, grad P^T                 -> Y1bar, Y2bar
+  Q8  y  D_y^T, S_y^T, [0,0] projection, Q_y^T        -> Xbar
+  Q7  x  per-eigenvalue transposed sweep             -> R2bar
+  Q6  y  H_y^T                                       -> R1bar
+  Q5  x  B_x^T, -nu pres-bar, divergence^T           -> W1bar, W2bar
+  Q4  y  S_y^T, D_y^T, A_y^-T, B_y^T, (B S)_y^T      -> Q1bar, Q2bar
+  Q3s x  A_x^-T, B_x^T, (B S)_x^T                    -> RHSbar, Ubar Vbar Tbar (old-time part)
+  Q3  x  forward-DCT_x^T, pressure / buoyancy terms  -> Cbar, DPZbar, TSYbar, pres-bar
+  Q2a y  ux, uz; products^T for U, V; DCT_y^T chains -> A_F*bar, uxbar, uzbar (partial)
+  Q2b y  products^T for T; ux/uz chains; D_y^T, S_y^T -> A_F*bar, pres-bar, Tbar
+  Q1  x  DCT_x^T, D_x^T, S_x^T                       -> Ubar, Vbar, Tbar (convection part)
+
+The gradient arrays are updated in place: they hold d/d(new state) on entry
+and d/d(old state) on exit, so a horizon is a loop of adjoint steps over the
+forward states taken in reverse order.
+"""
+import torch
+
+from .. import _lib
+from .._dev import DTYPE, device, to_dev
+from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX, P_MDTSZ,
+                    P_MNU, FusedBatch, Prog, _candidates, _Instance, _pick, build_programs, host_tables)
+
+BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
+
+
+def build_adjoint_programs(tkind, fft):
+    """R1 and the twelve transposed passes of one IMEX Euler step (beta = 1)."""
+    BWD, BWD_T, FWD_T = _lib.DCT_BWD, _lib.DCT_BWD_T, _lib.DCT_FWD_T
+    kinds = {"U": "CD", "V": "CD", "T": tkind}
+    ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
+    Q = []
+
+    r1 = build_programs(tkind, fft)[0]
+    r1.name = "R1"
+    Q.append(r1)
+
+    # Q10 (y, N-2 lines): U = U* - T_y S_y^T G1 (and V)
+    p = Prog("Q10", 1, L_NG, 2)
+    for i, F in enumerate("UV"):
+        p.load(i, "b" + F + "G", L_MG)
+        p.store(i, "b" + F + "S")
+        p.scale(i, alpha=-1.0)
+    p.tdma_multi(0, 2, "CD")
+    p.stencil(0, "CD")
+    p.stencil(1, "CD")
+    p.store(0, "bG1")
+    p.store(1, "bG2")
+    Q.append(p)
+
+    # Q9 (x, M lines): pres += S_x Y1 / dt; G1 = T_x S_x^T D_x S_x Y1 / sx; G2 = T_x S_x^T S_x Y2
+    p = Prog("Q9", 0, L_M, 2)
+    p.load(0, "bG1", L_NG)
+    p.load(1, "bG2", L_NG)
+    p.tdma_multi(0, 2, "CD")
+    p.stencil(0, "CD")
+    p.stencil(1, "CD")
+    p.scale(0, par=P_ISX)
+    p.diff_t(0)
+    p.load_add(0, "bPRES", par=P_IDT)
+    p.stencil_t(0, "CN")
+    p.stencil_t(1, "CN")
+    p.store(0, "bY1")
+    p.store(1, "bY2")
+    Q.append(p)
+
+    # Q8 (y, N-2 lines): PG = Z Q_y X; Y1 = S_y PG; Y2 = D_y Y1 / sz
+    p = Prog("Q8", 1, L_NG, 1)
+    p.load(0, "bY2", L_M)
+    p.scale(0, par=P_ISZ)
+    p.diff_t(0)
+    p.load_add(0, "bY1")
+    p.stencil_t(0, "CN")
+    p.add("ZERO00", 0)
+    p.dense(0, "QyT", L_MG)
+    p.store(0, "bX")
+    Q.append(p)
+
+    # Q7 (x, M-2 lines): transposed per-eigenvalue sweep
+    p = Prog("Q7", 0, L_MG, 1)
+    p.load(0, "bX", L_NG)
+    p.add("POISSON_T", 0, mat="Pois")
+    p.store(0, "bR2")
+    Q.append(p)
+
+    # Q6 (y, N-2 lines): H_y^T
+    p = Prog("Q6", 1, L_NG, 1)
+    p.load(0, "bR2", L_MG)
+    p.dense(0, "HyT", L_M)
+    p.store(0, "bR1")
+    Q.append(p)
+
+    # Q5 (x, M lines): div = D_x S_x W1 / sx + S_x W2; pres -= nu div; R1 = B_x div
+    p = Prog("Q5", 0, L_M, 2)
+    p.load(0, "bR1", L_NG)
+    p.banded(0, "BxT", -4, 3, L_N)
+    p.load_add(0, "bPRES", par=P_MNU)
+    p.copy(1, 0)
+    p.stencil_t(1, "CD")
+    p.store(1, "bW2")
+    p.scale(0, par=P_ISX)
+    p.diff_t(0)
+    p.stencil_t(0, "CD")
+    p.store(0, "bW1")
+    Q.append(p)
+
+    # Q4 (y, N-2 lines): F* = A_y^-1 (B_y Q1 + (B S)_y Q2); W1 = S_y U*; W2 = D_y S_y V* / sz
+    p = Prog("Q4", 1, L_NG, 4)
+    p.load(0, "bUS", L_MG)
+    p.load(3, "bW1", L_M)
+    p.stencil_t(3, "CD")
+    p.axpy(0, 3)
+    p.load(1, "bVS", L_MG)
+    p.load(3, "bW2", L_M)
+    p.scale(3, par=P_ISZ)
+    p.diff_t(3)
+    p.stencil_t(3, "CD")
+    p.axpy(1, 3)
+    p.load(2, "bTG", L_MG)
+    p.fdma_t(0, ["Ay_U", "Ay_U", "Ay_T"])
+    for i, F in enumerate("UVT"):
+        p.copy(3, i)
+        p.banded(3, "BSyT", -4, 4, L_MG)
+        p.store(3, "bQ2_" + F)
+        p.banded(i, "ByT", -4, 3, L_M)
+        p.store(i, "bQ1_" + F)
+    Q.append(p)
+
+    # Q3s (x, M lines): Q1 = A_x^-1 B_x RHS; Q2 = A_x^-1 (B S)_x F  (starts the state gradient)
+    p = Prog("Q3s", 0, L_M, 6)
+    for i, F in enumerate("UVT"):
+        p.load(i, "bQ1_" + F, L_NG)
+        p.load(3 + i, "bQ2_" + F, L_NG)
+    p.fdma_t(0, [ax[F] for F in "UVT"] * 2)
+    for i, F in enumerate("UVT"):
+        p.banded(i, "BxT", -4, 3, L_N)
+        p.store(i, "bRHS_" + F)
+        p.banded(3 + i, "BSx_TT" if F == "T" else "BSx_UT", -4, 4, L_NG)
+        p.store(3 + i, "b" + F + "G")
+    Q.append(p)
+
+    # Q3 (x, M lines): RHS = -dt Fwd_x C (+ pressure gradient, buoyancy, lift terms)
+    p = Prog("Q3", 0, L_M, 2)
+    for F in "UVT":
+        p.load(0, "bRHS_" + F, L_N)
+        if F == "U":
+            p.copy(1, 0)
+            p.scale(1, par=P_MDTSX)
+            p.diff_t(1)
+            p.store_add(1, "bPRES")
+        elif F == "V":
+            p.copy(1, 0)
+            p.scale(1, par=P_MDTSZ)
+            p.store(1, "bDPZ")
+            p.copy(1, 0)
+            p.scale(1, par=P_DT)
+            p.stencil_t(1, tkind)
+            p.store(1, "bTSY")
+        p.scale(0, par=P_MDT)
+        p.setlen(0, L_ND)
+        p.dct(0, FWD_T, fft)
+        p.store(0, "bC_" + F)
+    Q.append(p)
+
+    # Q2a / Q2b (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised
+    def velocities(p):
+        for s, F in ((0, "U"), (1, "V")):
+            p.load(s, "A_" + F + "0", L_MG)
+            p.stencil(s, "CD")
+            p.setlen(s, L_MD)
+            p.dct(s, BWD, fft)
+
+    def products_t(p, F, first):
+        p.load(4, "bC_" + F, L_M)
+        p.setlen(4, L_MD)
+        p.dct(4, FWD_T, fft)                      # conv bar
+        p.load(5, "A_" + F + "x", L_MG)
+        p.stencil(5, "CD")
+        p.setlen(5, L_MD)
+        p.dct(5, BWD, fft)                        # dF/dx (physical)
+        p.load(6, "A_" + F + "0", L_MG)
+        p.stencil(6, "CD")
+        p.diff(6)
+        p.scale(6, par=P_ISZ)
+        p.setlen(6, L_MD)
+        p.dct(6, BWD, fft)                        # dF/dz (physical)
+        p.mul(5, 4)
+        p.mul(6, 4)
+        if first:
+            p.copy(2, 5)
+            p.copy(3, 6)
+        else:
+            p.axpy(2, 5)
+            p.axpy(3, 6)
+        if F == "T":
+            p.load(6, "DTB1", L_MD)
+            p.mul(6, 4)
+            p.axpy(3, 6)
+        p.copy(5, 4)
+        p.mul(5, 0)                               # dF/dx bar = conv bar * ux
+        p.mul(4, 1)                               # dF/dz bar = conv bar * uz
+        p.dct(5, BWD_T, fft)
+        p.setlen(5, L_M)
+        p.stencil_t(5, "CD")
+        p.store(5, "bA_" + F + "x")
+        p.dct(4, BWD_T, fft)
+        p.setlen(4, L_M)
+        p.scale(4, par=P_ISZ)
+        p.diff_t(4)
+        p.stencil_t(4, "CD")
+        p.store(4, "bA_" + F + "0")
+
+    p = Prog("Q2a", 1, L_ND, 7)
+    velocities(p)
+    p.store(0, "UXP")
+    p.store(1, "UZP")
+    products_t(p, "U", True)
+    products_t(p, "V", False)
+    p.store(2, "bUXP")
+    p.store(3, "bUZP")
+    Q.append(p)
+
+    p = Prog("Q2b", 1, L_ND, 7)
+    p.load(0, "UXP", L_MD)
+    p.load(1, "UZP", L_MD)
+    p.load(2, "bUXP", L_MD)
+    p.load(3, "bUZP", L_MD)
+    products_t(p, "T", False)
+    for s, F in ((2, "U"), (3, "V")):
+        p.dct(s, BWD_T, fft)
+        p.setlen(s, L_M)
+        p.stencil_t(s, "CD")
+        p.store_add(s, "bA_" + F + "0")
+    p.load(4, "bDPZ", L_M)
+    p.diff_t(4)
+    p.store_add(4, "bPRES")
+    p.load(4, "bTSY", L_M)
+    p.stencil_t(4, "CD")
+    p.store_add(4, "bTG")
+    Q.append(p)
+
+    # Q1 (x, M-2 lines): A_F0 = Bwd_x S_x F; A_Fx = Bwd_x D_x S_x F / sx
+    p = Prog("Q1", 0, L_MG, 2)
+    for F in "UVT":
+        p.load(0, "bA_" + F + "0", L_ND)
+        p.dct(0, BWD_T, fft)
+        p.setlen(0, L_N)
+        p.load(1, "bA_" + F + "x", L_ND)
+        p.dct(1, BWD_T, fft)
+        p.setlen(1, L_N)
+        p.scale(1, par=P_ISX)
+        p.diff_t(1)
+        p.axpy(0, 1)
+        p.stencil_t(0, kinds[F])
+        p.store_add(0, "b" + F + "G")
+    Q.append(p)
+    return Q
+
+
+def adjoint_shapes(N, M, Nd, Md):
+    """Intermediate arrays of the adjoint passes (name -> shape)."""
+    sh = {}
+    for k in ("bUS", "bVS", "bX", "bR2"):
+        sh[k] = (N - 2, M - 2)
+    for k in ("bG1", "bG2", "bY1", "bY2", "bW1", "bW2", "bR1", "bTSY"):
+        sh[k] = (N - 2, M)
+    for F in "UVT":
+        sh["bQ1_" + F] = (N - 2, M)
+        sh["bQ2_" + F] = (N - 2, M - 2)
+        sh["bRHS_" + F] = (N, M)
+        sh["bC_" + F] = (Nd, M)
+        sh["bA_" + F + "0"] = (Nd, M - 2)
+        sh["bA_" + F + "x"] = (Nd, M - 2)
+    sh["bDPZ"] = (N, M)
+    for k in ("UXP", "UZP", "bUXP", "bUZP"):
+        sh[k] = (Nd, Md)
+    return sh
+
+
+def add_adjoint_buffers(I, bar_views):
+    """Gradient arrays, scratch and transposed operator tables of one instance."""
+    ns = I.ns
+    N, M, Nd, Md = I.N, I.M, I.Nd, I.Md
+    dev = device()
+    a = I.arrays
+    for k in BAR_STATE:
+        a[k] = bar_views[k]
+    for k, shp in adjoint_shapes(N, M, Nd, Md).items():
+        a[k] = torch.zeros(shp, dtype=DTYPE, device=dev)
+    host = host_tables(N, M, ns.T.xs[0].id, ns.dt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd, adjoint=True)
+    for k in ("BxT", "ByT", "BSx_UT", "BSx_TT", "BSyT", "HyT", "QyT"):
+        I.tables[k] = to_dev(host[k])
+
+
+class FusedAdjoint(FusedBatch):
+    """Forward and reverse fused steps for a batch of instances.
+
+    ``state_arena`` holds the forward state of every instance (U, V, T, P,
+    pres), ``bar_arena`` the gradient with respect to it, in the same layout.
+    ``adjoint_step()`` replaces the gradient w.r.t. the state after one step
+    taken from the current ``state_arena`` by the gradient w.r.t. that state.
+    """
+
+    def __init__(self, solvers):
+        FusedBatch.__init__(self, solvers)
+        self.bar_arena = torch.zeros_like(self.state_arena)
+        off = 0
+        for I in self.insts:
+            views = {}
+            for key in _Instance.STATE:
+                r, c = I.arrays[key].shape
+                views["b" + key] = self.bar_arena[off:off + r * c].view(r, c)
+                off += r * c
+            add_adjoint_buffers(I, views)
+        tkind = self.solvers[0].T.xs[0].id
+        self.aprogs = build_adjoint_programs(tkind, self.fft)
+        self.alaunches = [self._default_launch(p) for p in self.aprogs]
+        self.agraph = None
+
+    def _default_launch(self, prog):
+        lines, lcap, fft_n = self._pass_geometry(prog)
+        tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
+        return self._launch(prog, tb, nt)
+
+    def run_adjoint_pass(self, i):
+        name, P, d_insts, d_work, nwork = self.alaunches[i]
+        import ctypes
+        from .._dev import stream
+        _lib.check(_lib.lib().pgx_run_batched(ctypes.byref(P), d_insts.data_ptr(), d_work.data_ptr(), nwork,
+                                              stream()), name)
+
+    def adjoint_step_eager(self):
+        for i in range(len(self.alaunches)):
+            self.run_adjoint_pass(i)
+
+    def adjoint_step(self):
+        if self.agraph is not None:
+            self.agraph.replay()
+        else:
+            self.adjoint_step_eager()
+
+    def autotune_adjoint(self, reps=3, verbose=False):
+        """Per-pass tile choice for the adjoint passes (state and gradients restored after)."""
+        saved_s, saved_b = self.state_arena.clone(), self.bar_arena.clone()
+        stream = torch.cuda.current_stream()
+        chosen = {}
+        for i, prog in enumerate(self.aprogs):
+            lines, lcap, fft_n = self._pass_geometry(prog)
+            d_insts = self.alaunches[i][2]
+            best = None
+            for tb, nt in _candidates(prog, sum(lines), lcap, fft_n, max(lines)):
+                L = self._launch(prog, tb, nt, d_insts)
+                self.alaunches[i] = L
+                self.run_adjoint_pass(i)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(reps):
+                    self.run_adjoint_pass(i)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / reps
+                if verbose:
+                    print(prog.name, tb, nt, round(ms, 4))
+                if best is None or ms < best[0]:
+                    best = (ms, L, tb, nt)
+            self.alaunches[i] = best[1]
+            chosen[prog.name] = (best[2], best[3], round(best[0], 4))
+        self.state_arena.copy_(saved_s)
+        self.bar_arena.copy_(saved_b)
+        torch.cuda.synchronize()
+        self.agraph = None
+        self.atuned = chosen
+        return chosen
+
+    def capture_adjoint(self):
+        """Record one adjoint step in a CUDA graph (``adjoint_step()`` then replays it)."""
+        saved_s, saved_b = self.state_arena.clone(), self.bar_arena.clone()
+        self.adjoint_step_eager()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.adjoint_step_eager()
+        torch.cuda.synchronize()
+        self.state_arena.copy_(saved_s)
+        self.bar_arena.copy_(saved_b)
+        self.agraph = g
+
+    # -- views of the per-instance state in the arenas
+    def views(self, arena, keys=("UG", "VG", "TG")):
+        out, off = [], 0
+        for I in self.insts:
+            d = {}
+            for key in _Instance.STATE:
+                r, c = I.arrays[key].shape
+                if key in keys:
+                    d[key] = arena[off:off + r * c].view(r, c)
+                off += r * c
+            out.append(d)
+        return out
+
+
+class HorizonGradient:
+    """Value and gradient of J_i(X_i) = ||Phi^H(X_i) - X_i||_2 for every instance of a batch,
+    X = (U, V, T) with the pressure (and P) starting from zero, by the fused adjoint.
+
+    Forward states are checkpointed every ``every`` steps during the forward
+    sweep; in the reverse sweep each segment is recomputed (``every`` fused
+    steps, states kept in ``traj``) and then stepped back with the adjoint.
+    """
+
+    def __init__(self, fa, nsteps, every=20):
+        self.fa, self.H, self.every = fa, nsteps, every
+        n = fa.state_arena.numel()
+        self.nseg = -(-nsteps // every)
+        dev = fa.state_arena.device
+        self.ckpt = torch.zeros((self.nseg, n), dtype=DTYPE, device=dev)
+        self.traj = torch.zeros((every, n), dtype=DTYPE, device=dev)
+        self.x0 = torch.zeros(n, dtype=DTYPE, device=dev)
+        self.graphs = {}
+        self._mask = torch.zeros(n, dtype=DTYPE, device=dev)
+        for d in fa.views(self._mask):
+            for v in d.values():
+                v.fill_(1.0)
+
+    def _seg_len(self, s):
+        return min(self.every, self.H - s * self.every)
+
+    def _forward(self):
+        fa = self.fa
+        for s in range(self.nseg):
+            self.ckpt[s].copy_(fa.state_arena)
+            for _ in range(self._seg_len(s)):
+                fa.step()
+
+    def _segment_reverse(self, k):
+        fa = self.fa
+        for j in range(k):
+            self.traj[j].copy_(fa.state_arena)
+            if j + 1 < k:
+                fa.step()
+        for j in reversed(range(k)):
+            fa.state_arena.copy_(self.traj[j])
+            fa.adjoint_step()
+
+    def _objective(self):
+        """r = (Phi^H(X) - X) on U, V, T; J per instance; seeds bar = r / J."""
+        fa = self.fa
+        r = (fa.state_arena - self.x0) * self._mask
+        J = []
+        for d in fa.views(r):
+            J.append(torch.sqrt(sum((v * v).sum() for v in d.values())))
+        J = torch.stack(J)
+        scale = torch.zeros_like(r)
+        for d, j in zip(fa.views(scale), J):
+            for v in d.values():
+                v.fill_(0.0)
+                v.add_(1.0 / j)
+        seed = r * scale
+        return J, seed
+
+    def value(self, X):
+        """J for the initial states X (an arena-shaped tensor; pressure entries are ignored)."""
+        fa = self.fa
+        self.x0.copy_(X * self._mask)
+        fa.state_arena.copy_(self.x0)
+        for _ in range(self.H):
+            fa.step()
+        return self._objective()[0]
+
+    def value_and_grad(self, X):
+        """(J per instance, dJ/dX arena-shaped: U, V, T entries; zero elsewhere)."""
+        fa = self.fa
+        self.x0.copy_(X * self._mask)
+        fa.state_arena.copy_(self.x0)
+        self._forward()
+        J, seed = self._objective()
+        fa.bar_arena.copy_(seed)
+        for s in reversed(range(self.nseg)):
+            fa.state_arena.copy_(self.ckpt[s])
+            self._segment_reverse(self._seg_len(s))
+        g = (fa.bar_arena - seed) * self._mask
+        return J, g

@@ -116,6 +116,7 @@ class Plan_numpy(MetaPlan):
 class _InPlaceBanded(MetaPlan):
     def _sweep(self, b, fn):
         axis = self.axis if b.dim() == 2 else 0
+        self._check_b(b)
         p, s0, s1, _, nl = geom(b, axis)
         _lib.check(getattr(_lib.lib(), fn)(self._h, p, s0, s1, nl, axis, stream()), self.flags["method"])
         return b
@@ -209,6 +210,8 @@ class Plan_Poisson(MetaPlan):
         return self._sweep(b, "pgx_poisson_solve")
 
     def _sweep(self, b, fn):
+        if b.dim() != 2 or b.shape[self.axis] != self.N or b.shape[1 - self.axis] != self.alpha.size:
+            raise ValueError("poisson: array of shape {} does not match the plan".format(tuple(b.shape)))
         p, s0, s1, _, _ = geom(b, self.axis)
         _lib.check(getattr(_lib.lib(), fn)(self._h, p, s0, s1, self.axis, stream()), "poisson")
         return b

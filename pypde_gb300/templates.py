@@ -63,10 +63,25 @@ def solverplan_poisson2d(bases, singular=False, scale=(1, 1)):
     """Fast-diagonalisation 2-D Poisson plan (poisson.py:43-110)."""
     field = Field(bases)
     assert field.ndim == 2
-    Sx, Bx, Ix = _axis_mats(field.xs[0])
+    fd = poisson2d_matrices(_axis_mats(field.xs[0]), _axis_mats(field.xs[1]), singular, scale)
+    Ax, Cx, wy, Qy, Hy, Bx = (fd[k] for k in ("Ax", "Cx", "wy", "Qy", "Hy", "Bx"))
+    solver = SolverPlan()
+    solver.add_rhs(PlanRHS(Bx, ndim=2, axis=0))
+    solver.add_rhs(PlanRHS(Hy, ndim=2, axis=1))
+    solver.add_lhs(PlanLHS(Ax, alpha=wy, C=Cx, ndim=2, axis=0, method="poisson", singular=True))
+    solver.add_lhs(PlanLHS(Qy, ndim=2, axis=1, method="multiply"))
+    solver._fd = fd
+    return solver
+
+
+def poisson2d_matrices(mx, my, singular=False, scale=(1, 1)):
+    """Host matrices of the fast-diagonalisation plan (poisson.py:43-110) from the
+    (S, B, I) triples of the two axes: Ax, Cx, the sorted eigenpairs wy / Qy of
+    Cy^-1 Ay and the right-hand-side operator Hy = Qy^-1 Cy^-1 By."""
+    Sx, Bx, Ix = mx
+    Sy, By, Iy = my
     Ax = Ix @ Sx * (1.0 / scale[0] ** 2.0)
     Cx = Bx @ Sx
-    Sy, By, Iy = _axis_mats(field.xs[1])
     Ay = Iy @ Sy * (1.0 / scale[1] ** 2.0)
     Cy = By @ Sy
     CyI = np.linalg.inv(Cy)
@@ -74,10 +89,4 @@ def solverplan_poisson2d(bases, singular=False, scale=(1, 1)):
     if singular:
         wy[0] += 1e-20
     Hy = QyI @ CyI @ By
-    solver = SolverPlan()
-    solver.add_rhs(PlanRHS(Bx, ndim=2, axis=0))
-    solver.add_rhs(PlanRHS(Hy, ndim=2, axis=1))
-    solver.add_lhs(PlanLHS(Ax, alpha=wy, C=Cx, ndim=2, axis=0, method="poisson", singular=True))
-    solver.add_lhs(PlanLHS(Qy, ndim=2, axis=1, method="multiply"))
-    solver._fd = dict(Ax=Ax, Cx=Cx, wy=wy, Qy=Qy, Hy=Hy, Bx=Bx)
-    return solver
+    return dict(Ax=Ax, Cx=Cx, wy=wy, Qy=Qy, Hy=Hy, Bx=Bx)

@@ -1,0 +1,159 @@
+"""The fused reverse-mode step (thirteen line-program passes) on the GPU.
+
+One adjoint step is compared with the autograd vector-Jacobian product of the
+plain step (whose every operator runs a hand-written transposed kernel):
+1e-10 relative.  The checkpointed horizon gradient is compared with the
+autograd horizon gradient (1e-9) and with central finite differences of the
+fused forward map, h = 1e-6 (1e-6 relative, the path's stated target).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+KEYS = (("TG", "T"), ("UG", "U"), ("VG", "V"), ("PRES", "pres"))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    return torch
+
+
+def _ns(case, shape, **kw):
+    from pypde_gb300.navier.rbc2d import NavierStokes
+    cfg = dict(ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", tsave=None)
+    cfg.update(kw)
+    return NavierStokes(case=case, shape=shape, **cfg)
+
+
+def _random_state(torch, ns, seed):
+    rng = np.random.default_rng(seed)
+    ns.set_temperature_noise(seed, 1e-2)
+    for F in (ns.U, ns.V):
+        F.vhat = torch.as_tensor(1e-2 * rng.uniform(-1, 1, tuple(F.vhat.shape)), device="cuda")
+    ns.pres.vhat = torch.as_tensor(1e-2 * rng.uniform(-1, 1, tuple(ns.pres.vhat.shape)), device="cuda")
+    return tuple(getattr(ns, k).vhat.clone() for k in ("T", "U", "V", "pres"))
+
+
+STEP_CASES = [("linear", (33, 33), True), ("rbc", (33, 17), True), ("linear", (24, 20), False),
+              ("linear", (65, 33), True), ("zero", (17, 33), True)]
+
+
+@pytest.mark.parametrize("case,shape,dealias", STEP_CASES, ids=[f"{c[0]}-{c[1][0]}x{c[1][1]}" for c in STEP_CASES])
+def test_adjoint_step_vs_autograd(torch, case, shape, dealias):
+    from pypde_gb300.navier.adjoint import step
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint
+    ns = _ns(case, shape, dealias=dealias)
+    X = _random_state(torch, ns, 5)
+    rng = np.random.default_rng(6)
+    gbar = [torch.as_tensor(rng.standard_normal(tuple(x.shape)), device="cuda") for x in X]
+    Xr = [x.clone().requires_grad_(True) for x in X]
+    with torch.enable_grad():
+        Y = step(ns, Xr)
+        ref = torch.autograd.grad(Y, Xr, gbar)
+    ns2 = _ns(case, shape, dealias=dealias)
+    for (k, f), x in zip(KEYS, X):
+        getattr(ns2, f).vhat = x.clone()
+    fa = FusedAdjoint([ns2])
+    bv = fa.views(fa.bar_arena, keys=("UG", "VG", "TG", "PRES"))[0]
+    for (k, _), g in zip(KEYS, gbar):
+        bv[k].copy_(g)
+    fa.adjoint_step_eager()
+    for (k, _), r in zip(KEYS, ref):
+        e = rel_err(bv[k].cpu().numpy(), r.cpu().numpy())
+        assert e < 1e-10, (k, e)
+
+
+def _arena_state(torch, fa, X3s):
+    Xa = torch.zeros_like(fa.state_arena)
+    for v, X3 in zip(fa.views(Xa), X3s):
+        for k, x in zip(("TG", "UG", "VG"), X3):
+            v[k].copy_(x)
+    return Xa
+
+
+def test_horizon_gradient_vs_autograd_and_fd(torch):
+    from pypde_gb300.navier.adjoint import ResidualObjective, random_directions
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    H, every = 12, 5
+    ns = _ns("linear", (33, 33))
+    X = _random_state(torch, ns, 3)[:3]
+    J_ref, g_ref = ResidualObjective(ns, H, every).value_and_grad(X)
+    fa = FusedAdjoint([_ns("linear", (33, 33))])
+    fa.capture(1)
+    fa.capture_adjoint()
+    hg = HorizonGradient(fa, H, every)
+    Xa = _arena_state(torch, fa, [X])
+    J, g = hg.value_and_grad(Xa)
+    assert abs(float(J[0]) - J_ref) / J_ref < 1e-10
+    gv = fa.views(g)[0]
+    for k, r in zip(("TG", "UG", "VG"), g_ref):
+        e = rel_err(gv[k].cpu().numpy(), r.cpu().numpy())
+        assert e < 1e-9, (k, e)
+    # central differences of the fused forward map, 3 random unit directions
+    dirs = random_directions([x.shape for x in X], 3, seed=21, device="cuda")
+    h = 1e-6
+    for d in dirs:
+        Da = _arena_state(torch, fa, [d])
+        fd = (float(hg.value(Xa + h * Da)[0]) - float(hg.value(Xa - h * Da)[0])) / (2 * h)
+        ad = float((g * Da).sum())
+        assert abs(fd - ad) / abs(ad) < 1e-6, (fd, ad)
+
+
+def test_batched_horizon_gradient_matches_single(torch):
+    """Instances of different sizes / Rayleigh numbers: the batch gives each instance's own gradient."""
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    specs = [((33, 33), 1e5, 1), ((65, 33), 3e5, 2), ((33, 17), 1e4, 3)]
+    H, every = 6, 4
+    Xs, singles = [], []
+    for shape, ra, seed in specs:
+        ns = _ns("linear", shape, ra=ra, dt=0.005)
+        Xs.append(_random_state(torch, ns, seed)[:3])
+        fa1 = FusedAdjoint([_ns("linear", shape, ra=ra, dt=0.005)])
+        hg1 = HorizonGradient(fa1, H, every)
+        J1, g1 = hg1.value_and_grad(_arena_state(torch, fa1, [Xs[-1]]))
+        singles.append((float(J1[0]), {k: v.clone() for k, v in fa1.views(g1)[0].items()}))
+    fa = FusedAdjoint([_ns("linear", s, ra=ra, dt=0.005) for s, ra, _ in specs])
+    fa.autotune(reps=1)
+    fa.autotune_adjoint(reps=1)
+    hg = HorizonGradient(fa, H, every)
+    J, g = hg.value_and_grad(_arena_state(torch, fa, Xs))
+    for i, (J1, g1) in enumerate(singles):
+        assert abs(float(J[i]) - J1) / J1 < 1e-12
+        for k, v in fa.views(g)[i].items():
+            assert rel_err(v.cpu().numpy(), g1[k].cpu().numpy()) < 1e-11, (i, k)
+
+
+def test_adjoint_step_vs_oracle_directional_derivative(torch):
+    """<g, Phi'(X) d> from the oracle's step (CPU, central differences) against <Phi'(X)^T g, d> on the GPU."""
+    from oracle import rbc2d as orb
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint
+    shape = (33, 33)
+    ns = _ns("linear", shape)
+    X = [x.cpu().numpy() for x in _random_state(torch, ns, 8)]
+    rng = np.random.default_rng(9)
+    d = [rng.standard_normal(x.shape) for x in X]
+    g = [rng.standard_normal(x.shape) for x in X]
+    ref = orb.NavierStokes(case="linear", shape=shape, ra=1e5, pr=1.0, dt=0.01, dealias=True, tsave=None)
+
+    def phi(sign, h=1e-4):
+        ref.That, ref.Uhat, ref.Vhat, ref.pres = [x + sign * h * e for x, e in zip(X, d)]
+        ref.update()
+        return [ref.That, ref.Uhat, ref.Vhat, ref.pres]
+
+    yp, ym = phi(+1), phi(-1)
+    lhs = sum(float((gi * (a - b)).sum()) / 2e-4 for gi, a, b in zip(g, yp, ym))
+    fa = FusedAdjoint([ns])
+    sv = fa.views(fa.state_arena, keys=("UG", "VG", "TG", "PRES"))[0]
+    bv = fa.views(fa.bar_arena, keys=("UG", "VG", "TG", "PRES"))[0]
+    for (k, _), x, gi in zip(KEYS, X, g):
+        sv[k].copy_(torch.as_tensor(x))
+        bv[k].copy_(torch.as_tensor(gi))
+    fa.adjoint_step()
+    rhs = sum(float((bv[k].cpu().numpy() * di).sum()) for (k, _), di in zip(KEYS, d))
+    assert abs(lhs - rhs) / abs(rhs) < 1e-8, (lhs, rhs)
