@@ -376,7 +376,77 @@ def run_gpu(args, rank, world):
         line["clocks"] = clk
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and args.adjoint_iters >= 0:
+        line["adjoint"] = run_adjoint(args, stream)
     return line
+
+
+def run_adjoint(args, stream):
+    """Adjoint steady-state search, 129 x 129, Ra 1e5, Pr 1, dt 0.01: J = ||Phi^200(X) - X|| from the
+    conductive state + 1e-2 U(-1,1) noise (seed 3), checkpoints every 20 steps; gradient by the fused
+    reverse-mode passes; central differences (h = 1e-6) on 20 random unit directions; descent."""
+    import torch
+    from pypde_gb300.navier.adjoint import descend, random_directions
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    from pypde_gb300.navier.rbc2d import NavierStokes
+    H, every, shape = args.adjoint_horizon, 20, (129, 129)
+    ns = NavierStokes(case="linear", shape=shape, ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu",
+                      tsave=None)
+    ns.set_temperature_noise(3, 1e-2)
+    fa = FusedAdjoint([ns])
+    fa.autotune(reps=2)
+    fa.autotune_adjoint(reps=2)
+    fa.capture(1)
+    fa.capture_adjoint()
+    hg = HorizonGradient(fa, H, every)
+    X = fa.state_arena.clone()
+    for _ in range(2):  # warm-up
+        hg.value_and_grad(X)
+    torch.cuda.synchronize()
+
+    def timed(fn, reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps, out
+
+    reps = max(2, min(args.steps, 5))
+    ms_j, _ = timed(lambda: hg.value(X), reps)
+    ms_g, (J, g) = timed(lambda: hg.value_and_grad(X), reps)
+    # per-step costs: one fused forward step and one adjoint step (graph replays)
+    ms_f1, _ = timed(fa.step, 50)
+    ms_a1, _ = timed(fa.adjoint_step, 50)
+    # central differences on 20 random unit directions of the (T, U, V) coefficient space
+    shapes = [v.shape for v in fa.views(X)[0].values()]
+    dirs = random_directions(shapes, 20, seed=17, device="cuda")
+    h, errs = 1e-6, []
+    for d in dirs:
+        D = torch.zeros_like(X)
+        for v, e in zip(fa.views(D)[0].values(), d):
+            v.copy_(e)
+        fd = (float(hg.value(X + h * D)[0]) - float(hg.value(X - h * D)[0])) / (2 * h)
+        ad = float((g * D).sum())
+        errs.append(abs(fd - ad) / abs(ad))
+    # steady-state search: descent iterations, one gradient evaluation each
+    t0 = time.perf_counter()
+    _, hist = descend(hg.value_and_grad, X, args.adjoint_iters)
+    torch.cuda.synchronize()
+    wall_desc = time.perf_counter() - t0
+    return {"config": "129x129, aspect 1, Ra 1e5, Pr 1, dt 0.01, horizon %d steps, checkpoint every %d, "
+                      "X0 = conductive + 1e-2 U(-1,1) (seed 3); J = ||Phi^H(X) - X||_2 over (T, U, V)" % (H, every),
+            "grads_per_s": round(1e3 / ms_g, 3), "ms_per_grad": round(ms_g, 3), "ms_per_objective": round(ms_j, 3),
+            "cost_ratio_grad_vs_forward": round(ms_g / ms_j, 3),
+            "ms_forward_step": round(ms_f1, 4), "ms_adjoint_step": round(ms_a1, 4),
+            "adjoint_launches_per_step": len(fa.alaunches),
+            "fd_check": {"directions": len(dirs), "h": h, "max_rel_err": max(errs),
+                         "median_rel_err": statistics.median(errs)},
+            "descent": {"iterations": args.adjoint_iters, "accepted": len(hist) - 1, "J_first": hist[0],
+                        "J_last": hist[-1], "wall_s": round(wall_desc, 3),
+                        "step": "alpha J / |grad J|^2, alpha adapted by acceptance"},
+            "J": float(J[0]), "autotuned_adjoint_tiles": fa.atuned}
 
 
 def run_microbench(args):
@@ -471,6 +541,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
+    ap.add_argument("--adjoint-horizon", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "pgx.h"
 
 // Complex elements per line pair in each FFT buffer for DCT lengths up to n:
@@ -876,13 +878,34 @@ extern "C" int64_t pgx_program_smem(const pgx_program* P) {
 }
 
 namespace pgx {
+// The dynamic shared-memory cap is an attribute of the kernel in the device's
+// context, shared by every host thread (the autograd engine launches from its
+// own thread): raise it once per device to the opt-in maximum -- it is only a
+// cap -- rather than track a per-thread high-water mark that another thread
+// could invalidate by setting a lower value.
+static int raise_smem_cap(const void* fn, int which) {
+  static std::mutex mu;
+  static bool done[2][64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[which][dev]) return 0;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e != cudaSuccess) return (int)e;
+  done[which][dev] = true;
+  return 0;
+}
+
 int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles) {
   int64_t smem = pgx_program_smem(P);
-  static thread_local int64_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(line_program_single, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    configured = smem;
+  if (smem > 48 * 1024) {
+    int e = raise_smem_cap((const void*)line_program_single, 0);
+    if (e) return e;
   }
   line_program_single<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
   return (int)cudaGetLastError();
@@ -891,11 +914,9 @@ int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, i
 int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
                    cudaStream_t s) {
   int64_t smem = pgx_program_smem(P) + ((sizeof(pgx_instance) + 15) / 16) * 16;
-  static thread_local int64_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(line_program_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    configured = smem;
+  if (smem > 48 * 1024) {
+    int e = raise_smem_cap((const void*)line_program_batched, 1);
+    if (e) return e;
   }
   line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
   return (int)cudaGetLastError();

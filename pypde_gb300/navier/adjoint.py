@@ -110,14 +110,38 @@ def fd_check(obj, X3, directions, h=1e-6):
     return J, rows
 
 
-def descend(obj, X3, iters, lr, callback=None):
-    """Steady-state search: plain gradient descent on J with a fixed step ``lr``."""
-    X3 = tuple(x.detach().clone() for x in X3)
-    hist = []
+def _as_tuple(X):
+    return tuple(X) if isinstance(X, (tuple, list)) else (X,)
+
+
+def descend(value_and_grad, X, iters, alpha=0.5, callback=None):
+    """Steady-state search: gradient descent on J with the step alpha J / |grad J|^2 (the step that
+    would zero a linear J), enlarged after an accepted step and halved after a rejected one.
+
+    ``value_and_grad(X) -> (J, grad)`` with X a tensor or a tuple of tensors (J a scalar or a
+    one-element tensor).  Returns (X, [J of every accepted iterate])."""
+    single = not isinstance(X, (tuple, list))
+    X = tuple(x.detach().clone() for x in _as_tuple(X))
+
+    def vg(Y):
+        J, g = value_and_grad(Y[0] if single else Y)
+        return float(J if not torch.is_tensor(J) else J.reshape(-1)[0]), _as_tuple(g)
+
+    J, g = vg(X)
+    hist = [J]
     for it in range(iters):
-        J, g = obj.value_and_grad(X3)
-        hist.append(J)
-        X3 = tuple(x - lr * gi for x, gi in zip(X3, g))
+        gn2 = sum(float((gi * gi).sum()) for gi in g)
+        if gn2 == 0.0 or J == 0.0:
+            break
+        t = alpha * J / gn2
+        Xn = tuple(x - t * gi for x, gi in zip(X, g))
+        Jn, gn = vg(Xn)
+        if Jn < J:
+            X, J, g = Xn, Jn, gn
+            alpha = min(1.0, 1.5 * alpha)
+            hist.append(J)
+        else:
+            alpha *= 0.5
         if callback is not None:
             callback(it, J)
-    return X3, hist
+    return (X[0] if single else X), hist
