@@ -492,31 +492,39 @@ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_doub
 //   FWD_T (-1)^j / (2N), w_k;  BWD_T 1 / w_j, (-1)^k   (w = 1 at both ends, 2 inside;
 // the transposed modes are the exact adjoints of FWD and BWD because C^T = W C W^-1).
 // Every pre-scale is symmetric in j <-> N - j for even N.
-__device__ __forceinline__ double dct_pre(int mode, int j, int N) {
-  const bool end = (j == 0 || j == N);
-  const double sg = (j & 1) ? -1.0 : 1.0;
-  switch (mode) {
-    case PGX_DCT_BWD: return end ? sg : 0.5 * sg;
-    case PGX_DCT_FWD_T: return sg * (0.5 / N);
-    case PGX_DCT_BWD_T: return end ? 1.0 : 0.5;
-    default: return 1.0;
+// Carried as (mode, 1/N): one division per op, the inner loops only select.
+struct DctScale {
+  int mode;
+  double invN;
+  bool has_pre, has_post;
+  __device__ __forceinline__ double pre(int j, int N) const {
+    const bool end = (j == 0 || j == N);
+    const double sg = (j & 1) ? -1.0 : 1.0;
+    switch (mode) {
+      case PGX_DCT_BWD: return end ? sg : 0.5 * sg;
+      case PGX_DCT_FWD_T: return sg * (0.5 * invN);
+      case PGX_DCT_BWD_T: return end ? 1.0 : 0.5;
+      default: return 1.0;
+    }
   }
-}
-__device__ __forceinline__ double dct_post(int mode, int k, int N) {
-  const bool end = (k == 0 || k == N);
-  const double sg = (k & 1) ? -1.0 : 1.0;
-  switch (mode) {
-    case PGX_DCT_FWD: return sg * (end ? 0.5 / N : 1.0 / N);
-    case PGX_DCT_FWD_T: return end ? 1.0 : 2.0;
-    case PGX_DCT_BWD_T: return sg;
-    default: return 1.0;
+  __device__ __forceinline__ double post(int k, int N) const {
+    const bool end = (k == 0 || k == N);
+    const double sg = (k & 1) ? -1.0 : 1.0;
+    switch (mode) {
+      case PGX_DCT_FWD: return sg * (end ? 0.5 * invN : invN);
+      case PGX_DCT_FWD_T: return end ? 1.0 : 2.0;
+      case PGX_DCT_BWD_T: return sg;
+      default: return 1.0;
+    }
   }
-}
-__device__ __forceinline__ bool dct_has_pre(int mode) {
-  return mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
-}
-__device__ __forceinline__ bool dct_has_post(int mode) {
-  return mode == PGX_DCT_FWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
+};
+__device__ __forceinline__ DctScale dct_scale(int mode, int N) {
+  DctScale s;
+  s.mode = mode;
+  s.invN = 1.0 / N;
+  s.has_pre = mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
+  s.has_post = mode == PGX_DCT_FWD || mode == PGX_DCT_FWD_T || mode == PGX_DCT_BWD_T;
+  return s;
 }
 
 // One radix-R Stockham stage over `npairs` pairs of lines.
@@ -526,7 +534,8 @@ __device__ __forceinline__ bool dct_has_post(int mode) {
 //          forward post-scale (no extraction pass).
 template <int R, bool FIRST, bool LAST>
 __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src, double2* dst, const double2* tw,
-                                               int L, int Ns, int npairs, double* x, int mode, int tws = 1) {
+                                               int L, int Ns, int npairs, double* x, const DctScale& ds,
+                                               int tws = 1) {
   const int LR = L / R;
   const int step = tws * (L / (Ns * R));  // twiddle table holds exp(-2 pi i k / (tws L))
   const int N = L >> 1;
@@ -543,8 +552,8 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
         const int sidx = m <= N ? m : L - m;
         double a = x[t0 * c.lcap + sidx];
         double b = two ? x[(t0 + 1) * c.lcap + sidx] : 0.0;
-        if (dct_has_pre(mode)) {
-          const double w = dct_pre(mode, sidx, N);
+        if (ds.has_pre) {
+          const double w = ds.pre(sidx, N);
           a *= w;
           b *= w;
         }
@@ -584,8 +593,8 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
       if (LAST) {
         if (kk <= N) {
           double2 z = o[q];
-          if (dct_has_post(mode)) {
-            const double sc = dct_post(mode, kk, N);
+          if (ds.has_post) {
+            const double sc = ds.post(kk, N);
             z.x *= sc;
             z.y *= sc;
           }
@@ -608,10 +617,11 @@ __device__ __forceinline__ int next_radix(int rem) { return (rem & 3) == 0 ? 4 :
 
 template <bool FIRST, bool LAST>
 __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double2* src, double2* dst, const double2* tw,
-                                               int L, int Ns, int npairs, double* x, int mode, int tws = 1) {
-  if (R == 4) stockham_stage<4, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
-  else if (R == 2) stockham_stage<2, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
-  else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, mode, tws);
+                                               int L, int Ns, int npairs, double* x, const DctScale& ds,
+                                               int tws = 1) {
+  if (R == 4) stockham_stage<4, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, ds, tws);
+  else if (R == 2) stockham_stage<2, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, ds, tws);
+  else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, ds, tws);
 }
 
 // DCT-I for even N = n - 1, exploiting both the realness and the even symmetry
@@ -628,7 +638,7 @@ __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double
 __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
   const int N = n - 1, H = N / 2;
-  const int mode = op.k;
+  const DctScale ds = dct_scale(op.k, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, op.a);
   const int npairs = (c.tb + 1) >> 1;
@@ -638,7 +648,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     const int t0 = 2 * pr;
     const bool two = t0 + 1 < c.tb;
     const double sn = -__ldg(&tw[j].y);
-    const double sg = dct_has_pre(mode) ? dct_pre(mode, j, N) : 1.0;
+    const double sg = ds.has_pre ? ds.pre(j, N) : 1.0;
     const double a0 = x[t0 * c.lcap + j], a1 = x[t0 * c.lcap + N - j];
     double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
     double ub = 0.0;
@@ -646,7 +656,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       const double b0 = x[(t0 + 1) * c.lcap + j], b1 = x[(t0 + 1) * c.lcap + N - j];
       ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
     }
-    if (dct_has_pre(mode)) {
+    if (ds.has_pre) {
       ua *= sg;
       ub *= sg;
     }
@@ -660,12 +670,12 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       double acc = 0.0;
       for (int j = 1 + lane; j < H; j += 32) {
         double d = xl[j] - xl[N - j];
-        if (dct_has_pre(mode)) d *= dct_pre(mode, j, N);
+        if (ds.has_pre) d *= ds.pre(j, N);
         acc = fma(__ldg(&tw[j].x), d, acc);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      const double d0 = (xl[0] - xl[N]) * (dct_has_pre(mode) ? dct_pre(mode, 0, N) : 1.0);
+      const double d0 = (xl[0] - xl[N]) * (ds.has_pre ? ds.pre(0, N) : 1.0);
       if (lane == 0) c.ybuf[t] = fma(2.0, acc, d0);
     }
   }
@@ -675,7 +685,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   int cur = 0, Ns = 1;
   for (int rem = N; rem > 1;) {
     const int R = next_radix(rem);
-    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, npairs, x, mode, 2);
+    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, npairs, x, ds, 2);
     cur ^= 1;
     Ns *= R;
     rem /= R;
@@ -690,8 +700,8 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     const double2 zm = Z[pr * c.fft_stride + m];
     const double2 zn = Z[pr * c.fft_stride + (m == 0 ? 0 : N - m)];
     double ya = zm.x + zn.x, yb = zm.y + zn.y;
-    if (dct_has_post(mode)) {
-      const double sc = dct_post(mode, 2 * m, N);
+    if (ds.has_post) {
+      const double sc = ds.post(2 * m, N);
       ya *= sc;
       yb *= sc;
     }
@@ -710,7 +720,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
     const int chunk = (H + 31) / 32;
-    const double osc = dct_has_post(mode) ? dct_post(mode, 1, N) : 1.0;  // the same for every odd k < N
+    const double osc = ds.has_post ? ds.post(1, N) : 1.0;  // the same for every odd k < N
     for (int t = warp; t < c.tb; t += nw) {
       double* xl = x + t * c.lcap;
       const int m0 = lane * chunk, m1 = min(m0 + chunk, H);
@@ -744,7 +754,7 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     return;
   }
   const int N = n - 1, L = 2 * N;
-  const int mode = op.k;
+  const DctScale ds = dct_scale(op.k, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, op.a);
   const int npairs = (c.tb + 1) >> 1;
@@ -758,9 +768,9 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     double2* dst = bufs[cur ^ 1];
     if (s == 0) {
       if (nst == 1) {
-        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, mode);
+        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, ds);
       } else {
-        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, mode);
+        stage_dispatch<true, false>(R, c, nullptr, c.f0, tw, L, Ns, npairs, x, ds);
         cur = 0;
         Ns *= R;
         rem /= R;
@@ -768,9 +778,9 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
         continue;
       }
     } else if (s == nst - 1) {
-      stage_dispatch<false, true>(R, c, src, nullptr, tw, L, Ns, npairs, x, mode);
+      stage_dispatch<false, true>(R, c, src, nullptr, tw, L, Ns, npairs, x, ds);
     } else {
-      stage_dispatch<false, false>(R, c, src, dst, tw, L, Ns, npairs, x, mode);
+      stage_dispatch<false, false>(R, c, src, dst, tw, L, Ns, npairs, x, ds);
       cur ^= 1;
     }
     Ns *= R;
@@ -782,7 +792,7 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       int t = idx / n, k = idx - t * n;
       double2 z = c.f0[(t >> 1) * c.fft_stride + k];
       double y = (t & 1) ? z.y : z.x;
-      if (dct_has_post(mode)) y *= dct_post(mode, k, N);
+      if (ds.has_post) y *= ds.post(k, N);
       x[t * c.lcap + k] = y;
     }
   }

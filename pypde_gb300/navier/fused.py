@@ -523,7 +523,7 @@ class _Instance:
         return {"UG": (N - 2, M - 2), "VG": (N - 2, M - 2), "TG": (N - 2, M - 2), "PG": (N - 2, M - 2),
                 "PRES": (N, M)}
 
-    def __init__(self, ns, fft, views=None):
+    def __init__(self, ns, fft, views=None, bind=True):
         if ns.nstage != 1 or ns.beta != 1.0:
             raise NotImplementedError("the fused step covers IMEX Euler with beta = 1; use update() otherwise")
         self.ns = ns
@@ -534,12 +534,15 @@ class _Instance:
         z = lambda r, c: torch.zeros((r, c), dtype=DTYPE, device=dev)  # noqa: E731
         a = {}
         # state (shared with the NavierStokes object's fields)
+        # (bind=False: a private copy, e.g. a second working set of the same instance)
         for key, fld in (("UG", ns.U), ("VG", ns.V), ("TG", ns.T), ("PG", ns.P), ("PRES", ns.pres)):
             if views is not None:
                 views[key].copy_(fld.vhat)
-                fld.vhat = a[key] = views[key]
+                a[key] = views[key]
             else:
-                fld.vhat = a[key] = fld.vhat.contiguous()
+                a[key] = fld.vhat.contiguous() if bind else fld.vhat.clone()
+            if bind:
+                fld.vhat = a[key]
         a["TBCC"] = ns.Tbc_cheby.contiguous()
         a["DTB1"] = ns.dTbcdz1.contiguous()
         a["DTB2"] = ns.dTbcdz2.contiguous()
@@ -693,7 +696,9 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
 class FusedBatch:
     """Fused Euler step for a batch of NavierStokes instances (any sizes / Ra)."""
 
-    def __init__(self, solvers):
+    def __init__(self, solvers, bind=True):
+        """``bind``: the solvers' fields become views of this batch's state arena (the default);
+        with bind=False the batch works on its own copy of the states."""
         self.solvers = list(solvers)
         tkinds = {ns.T.xs[0].id for ns in self.solvers}
         if len(tkinds) != 1:
@@ -711,7 +716,7 @@ class FusedBatch:
                 r, c = sh[key]
                 views[key] = self.state_arena[off:off + r * c].view(r, c)
                 off += r * c
-            self.insts.append(_Instance(ns, self.fft, views))
+            self.insts.append(_Instance(ns, self.fft, views, bind))
         self.progs = build_programs(tkinds.pop(), self.fft)
         self._build_launches()
         self.graph = None
@@ -743,12 +748,21 @@ class FusedBatch:
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=dev)
         return (prog.name, P, d_insts, d_work, len(work))
 
-    def _build_launches(self):
+    def _build_launches(self, tiles=None):
+        """Launch descriptors of the forward passes; ``tiles`` = {pass: (lines per CTA, threads)}
+        overrides the default choice (e.g. another batch's autotuned tiles)."""
         self.launches = []
         for prog in self.progs:
             lines, lcap, fft_n = self._pass_geometry(prog)
-            tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
+            if tiles and prog.name in tiles:
+                tb, nt = tiles[prog.name][:2]
+            else:
+                tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
             self.launches.append(self._launch(prog, tb, nt))
+
+    def tiles(self):
+        """{pass: (lines per CTA, threads)} of the current launches."""
+        return {L[0]: (L[1].tb, L[1].nthreads) for L in self.launches}
 
     def autotune(self, reps=3, verbose=False):
         """Time every candidate tile shape of every pass on this batch and keep the fastest.

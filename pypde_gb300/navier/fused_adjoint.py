@@ -424,79 +424,144 @@ class HorizonGradient:
     X = (U, V, T) with the pressure (and P) starting from zero, by the fused adjoint.
 
     Forward states are checkpointed every ``every`` steps during the forward
-    sweep; in the reverse sweep each segment is recomputed (``every`` fused
-    steps, states kept in ``traj``) and then stepped back with the adjoint.
+    sweep.  The reverse sweep recomputes each segment from its checkpoint
+    (``every`` fused steps, states kept in a trajectory buffer) and steps it
+    back with the adjoint passes.  With ``overlap`` the recomputation of
+    segment s-1 runs on a second stream, on a private working copy of the
+    batch, while the adjoint passes of segment s run on the main stream (two
+    trajectory buffers alternate); a single small instance leaves most SMs
+    idle in either sweep, so the two fill the GPU together.  With ``graph``
+    the whole evaluation (forward sweep, objective, reverse sweep, both
+    streams) is one CUDA graph: one replay per call.
     """
 
-    def __init__(self, fa, nsteps, every=20):
+    def __init__(self, fa, nsteps, every=20, overlap=True, graph=True):
         self.fa, self.H, self.every = fa, nsteps, every
+        self.overlap, self.use_graph = overlap, graph
         n = fa.state_arena.numel()
         self.nseg = -(-nsteps // every)
         dev = fa.state_arena.device
-        self.ckpt = torch.zeros((self.nseg, n), dtype=DTYPE, device=dev)
-        self.traj = torch.zeros((every, n), dtype=DTYPE, device=dev)
-        self.x0 = torch.zeros(n, dtype=DTYPE, device=dev)
-        self.graphs = {}
-        self._mask = torch.zeros(n, dtype=DTYPE, device=dev)
+        z = lambda *shape: torch.zeros(shape, dtype=DTYPE, device=dev)  # noqa: E731
+        self.ckpt = z(self.nseg, n)
+        self.traj = z(2 if overlap else 1, every, n)
+        self.x0, self.x_in, self.g_out = z(n), z(n), z(n)
+        self.J_out = z(len(fa.insts))
+        self._mask = z(n)
         for d in fa.views(self._mask):
             for v in d.values():
                 v.fill_(1.0)
+        self.rec = None
+        if overlap:
+            self.rec = FusedBatch(fa.solvers, bind=False)
+            self.rec._build_launches(fa.tiles())
+            self.side = torch.cuda.Stream(device=dev)
+        self.graphs = {}
 
     def _seg_len(self, s):
         return min(self.every, self.H - s * self.every)
 
-    def _forward(self):
+    # ---------------------------------------------------------------- pieces
+    def _forward_sweep(self, keep):
         fa = self.fa
+        fa.state_arena.copy_(self.x0)
         for s in range(self.nseg):
-            self.ckpt[s].copy_(fa.state_arena)
+            if keep:
+                self.ckpt[s].copy_(fa.state_arena)
             for _ in range(self._seg_len(s)):
-                fa.step()
-
-    def _segment_reverse(self, k):
-        fa = self.fa
-        for j in range(k):
-            self.traj[j].copy_(fa.state_arena)
-            if j + 1 < k:
-                fa.step()
-        for j in reversed(range(k)):
-            fa.state_arena.copy_(self.traj[j])
-            fa.adjoint_step()
+                fa.step_eager()
 
     def _objective(self):
-        """r = (Phi^H(X) - X) on U, V, T; J per instance; seeds bar = r / J."""
+        """r = (Phi^H(X) - X) on U, V, T; J per instance; returns (J, seed = r / J)."""
         fa = self.fa
         r = (fa.state_arena - self.x0) * self._mask
-        J = []
-        for d in fa.views(r):
-            J.append(torch.sqrt(sum((v * v).sum() for v in d.values())))
-        J = torch.stack(J)
+        J = torch.stack([torch.sqrt(sum((v * v).sum() for v in d.values())) for d in fa.views(r)])
         scale = torch.zeros_like(r)
         for d, j in zip(fa.views(scale), J):
             for v in d.values():
-                v.fill_(0.0)
-                v.add_(1.0 / j)
-        seed = r * scale
-        return J, seed
+                v.copy_((1.0 / j).expand_as(v))
+        return J, r * scale
 
-    def value(self, X):
-        """J for the initial states X (an arena-shaped tensor; pressure entries are ignored)."""
+    def _recompute(self, batch, s, buf):
+        """States at the start of every step of segment s into traj[buf] (batch: a working set)."""
+        k = self._seg_len(s)
+        batch.state_arena.copy_(self.ckpt[s])
+        for j in range(k):
+            self.traj[buf, j].copy_(batch.state_arena)
+            if j + 1 < k:
+                batch.step_eager()
+
+    def _reverse(self, s, buf):
         fa = self.fa
-        self.x0.copy_(X * self._mask)
-        fa.state_arena.copy_(self.x0)
-        for _ in range(self.H):
-            fa.step()
-        return self._objective()[0]
+        for j in reversed(range(self._seg_len(s))):
+            fa.state_arena.copy_(self.traj[buf, j])
+            fa.adjoint_step_eager()
+
+    def _reverse_sweep(self):
+        if not self.overlap:
+            for s in reversed(range(self.nseg)):
+                self._recompute(self.fa, s, 0)
+                self._reverse(s, 0)
+            return
+        main = torch.cuda.current_stream()
+        ready = [torch.cuda.Event() for _ in range(self.nseg)]
+        used = [torch.cuda.Event() for _ in range(self.nseg)]
+        fork = torch.cuda.Event()
+        fork.record(main)
+        self.side.wait_event(fork)
+
+        def issue_recompute(s):
+            with torch.cuda.stream(self.side):
+                if s + 2 < self.nseg:                  # traj[s % 2] was last read by segment s + 2
+                    self.side.wait_event(used[s + 2])
+                self._recompute(self.rec, s, s % 2)
+                ready[s].record(self.side)
+
+        last = self.nseg - 1
+        issue_recompute(last)
+        for s in reversed(range(self.nseg)):
+            if s - 1 >= 0:
+                issue_recompute(s - 1)
+            main.wait_event(ready[s])
+            self._reverse(s, s % 2)
+            used[s].record(main)
+        join = torch.cuda.Event()
+        join.record(self.side)
+        main.wait_event(join)
+
+    def _run(self, grad):
+        self._forward_sweep(keep=grad)
+        J, seed = self._objective()
+        self.J_out.copy_(J)
+        if grad:
+            self.fa.bar_arena.copy_(seed)
+            self._reverse_sweep()
+            self.g_out.copy_((self.fa.bar_arena - seed) * self._mask)
+
+    def _replay(self, grad):
+        if not self.use_graph:
+            self._run(grad)
+            return
+        g = self.graphs.get(grad)
+        if g is None:
+            self._run(grad)                 # warm-up outside the capture
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._run(grad)
+            self.graphs[grad] = g
+        g.replay()
+
+    # ------------------------------------------------------------------- API
+    def value(self, X):
+        """J per instance for the initial states X (arena-shaped; only U, V, T entries are used)."""
+        self.x_in.copy_(X)
+        self.x0.copy_(self.x_in * self._mask)
+        self._replay(False)
+        return self.J_out.clone()
 
     def value_and_grad(self, X):
         """(J per instance, dJ/dX arena-shaped: U, V, T entries; zero elsewhere)."""
-        fa = self.fa
-        self.x0.copy_(X * self._mask)
-        fa.state_arena.copy_(self.x0)
-        self._forward()
-        J, seed = self._objective()
-        fa.bar_arena.copy_(seed)
-        for s in reversed(range(self.nseg)):
-            fa.state_arena.copy_(self.ckpt[s])
-            self._segment_reverse(self._seg_len(s))
-        g = (fa.bar_arena - seed) * self._mask
-        return J, g
+        self.x_in.copy_(X)
+        self.x0.copy_(self.x_in * self._mask)
+        self._replay(True)
+        return self.J_out.clone(), self.g_out.clone()
