@@ -7,14 +7,17 @@ Pr = 1, aspect 1, dt = 0.005, IMEX Euler, 3/2 dealiasing, case "linear",
 T = conductive profile + 1e-3 U(-1,1) noise with seed 100 + i.
 
 A step = one time step of every instance (all 256), replayed from one CUDA
-graph of ten fused line-program launches.  ``value`` = instance-steps/s with
+graph of eleven fused line-program launches.  ``value`` = instance-steps/s with
 the state resident in HBM; ``e2e`` = the same through the public API with the
 state in pinned host memory (one H2D copy of every instance's state before and
 one D2H copy after each step, inside the timed region).  ``plain`` = the same
-instances run one by one on the per-instance GPU path.
+instances run one by one on the per-instance GPU path.  ``adjoint`` = the
+adjoint steady-state search (129 x 129, Ra 1e5, 200-step horizon, checkpoints
+every 20 steps): gradients/s, cost against the forward sweep, finite-difference
+check on 20 random directions, 50 descent iterations.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--instances 256] [--workload c4|c1|c3]
+                    [--instances 256] [--workload c4|c1|c3|c2|c5] [--adjoint-iters 50]
 Under torchrun every rank runs its own batch (weak scaling, no collective on
 the data path); rank 0 prints one JSON line.
 """
@@ -419,9 +422,9 @@ def run_adjoint(args, stream):
     # per-step costs: one fused forward step and one adjoint step (graph replays)
     ms_f1, _ = timed(fa.step, 50)
     ms_a1, _ = timed(fa.adjoint_step, 50)
-    # central differences on 20 random unit directions of the (T, U, V) coefficient space
+    # central differences on random unit directions of the (T, U, V) coefficient space
     shapes = [v.shape for v in fa.views(X)[0].values()]
-    dirs = random_directions(shapes, 20, seed=17, device="cuda")
+    dirs = random_directions(shapes, args.adjoint_fd, seed=17, device="cuda")
     h, errs = 1e-6, []
     for d in dirs:
         D = torch.zeros_like(X)
@@ -438,11 +441,13 @@ def run_adjoint(args, stream):
     return {"config": "129x129, aspect 1, Ra 1e5, Pr 1, dt 0.01, horizon %d steps, checkpoint every %d, "
                       "X0 = conductive + 1e-2 U(-1,1) (seed 3); J = ||Phi^H(X) - X||_2 over (T, U, V)" % (H, every),
             "grads_per_s": round(1e3 / ms_g, 3), "ms_per_grad": round(ms_g, 3), "ms_per_objective": round(ms_j, 3),
-            "cost_ratio_grad_vs_forward": round(ms_g / ms_j, 3),
+            "cost_ratio_grad_vs_forward": round(ms_g / min(ms_j, H * ms_f1), 3),
+            "cost_ratio_basis": "gradient (forward sweep + checkpointed reverse sweep, one graph) over the "
+                                "faster of: the objective's own graph, H single-step forward replays",
             "ms_forward_step": round(ms_f1, 4), "ms_adjoint_step": round(ms_a1, 4),
             "adjoint_launches_per_step": len(fa.alaunches),
-            "fd_check": {"directions": len(dirs), "h": h, "max_rel_err": max(errs),
-                         "median_rel_err": statistics.median(errs)},
+            "fd_check": {"directions": len(dirs), "h": h, "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": statistics.median(errs) if errs else None},
             "descent": {"iterations": args.adjoint_iters, "accepted": len(hist) - 1, "J_first": hist[0],
                         "J_last": hist[-1], "wall_s": round(wall_desc, 3),
                         "step": "alpha J / |grad J|^2, alpha adapted by acceptance"},
@@ -536,13 +541,14 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c4", choices=["c4", "c1", "c3", "c2"])
+    ap.add_argument("--workload", default="c4", choices=["c4", "c1", "c3", "c2", "c5"])
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
     ap.add_argument("--adjoint-horizon", type=int, default=200)
+    ap.add_argument("--adjoint-fd", type=int, default=20, help="finite-difference directions")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
@@ -550,6 +556,11 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.workload == "c2":
         print(json.dumps(run_microbench(args)))
+        return
+    if args.workload == "c5":  # the adjoint steady-state search alone
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"metric": METRIC, "adjoint": run_adjoint(args, torch.cuda.current_stream())}))
         return
     if args.impl == "reference":
         line = run_reference(args, rank, world)
