@@ -397,8 +397,18 @@ def run_adjoint(args, stream):
                       tsave=None)
     ns.set_temperature_noise(3, 1e-2)
     fa = FusedAdjoint([ns])
-    fa.autotune(reps=2)
-    fa.autotune_adjoint(reps=2)
+    if args.adjoint_profile:
+        # fixed launch order for a launch-list capture: forward steps, then adjoint steps (eager)
+        for _ in range(args.adjoint_profile):
+            fa.step_eager()
+        for _ in range(args.adjoint_profile):
+            fa.adjoint_step_eager()
+        torch.cuda.synchronize()
+        return {"profile_order": [p.name for p in fa.progs] * args.adjoint_profile +
+                                 [p.name for p in fa.aprogs] * args.adjoint_profile}
+    if not args.no_tune:
+        fa.autotune(reps=2)
+        fa.autotune_adjoint(reps=2)
     fa.capture(1)
     fa.capture_adjoint()
     hg = HorizonGradient(fa, H, every)
@@ -451,7 +461,7 @@ def run_adjoint(args, stream):
             "descent": {"iterations": args.adjoint_iters, "accepted": len(hist) - 1, "J_first": hist[0],
                         "J_last": hist[-1], "wall_s": round(wall_desc, 3),
                         "step": "alpha J / |grad J|^2, alpha adapted by acceptance"},
-            "J": float(J[0]), "autotuned_adjoint_tiles": fa.atuned}
+            "J": float(J[0]), "autotuned_adjoint_tiles": getattr(fa, "atuned", None)}
 
 
 def run_microbench(args):
@@ -549,6 +559,8 @@ def main():
     ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
     ap.add_argument("--adjoint-horizon", type=int, default=200)
     ap.add_argument("--adjoint-fd", type=int, default=20, help="finite-difference directions")
+    ap.add_argument("--adjoint-profile", type=int, default=0,
+                    help="c5 only: run N eager forward and N adjoint steps (fixed launch order) and exit")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
