@@ -240,7 +240,16 @@ def run_gpu(args, rank, world):
     solvers, fb = build_batch(specs)
     n_inst = len(solvers)
     stream = torch.cuda.current_stream()
-    tuned = fb.autotune() if not args.no_tune else None
+    tuned = None
+    if args.tiles:  # tiles saved by an earlier run (same workload): no tuning launches
+        with open(args.tiles) as f:
+            fb._build_launches(json.load(f)["forward"])
+        tuned = "loaded from %s" % args.tiles
+    elif not args.no_tune:
+        tuned = fb.autotune()
+    if args.save_tiles:
+        with open(args.save_tiles, "w") as f:
+            json.dump({"forward": fb.tiles()}, f)
     fb.capture(1)
     state_bytes = fb.state_arena.numel() * 8
     work_bytes = fb.scratch_bytes()
@@ -455,7 +464,7 @@ def run_adjoint(args, stream):
             "cost_ratio_basis": "gradient (forward sweep + checkpointed reverse sweep, one graph) over the "
                                 "faster of: the objective's own graph, H single-step forward replays",
             "ms_forward_step": round(ms_f1, 4), "ms_adjoint_step": round(ms_a1, 4),
-            "adjoint_launches_per_step": len(fa.alaunches),
+            "adjoint_launches_per_step": fa.adjoint_launches_per_step,
             "fd_check": {"directions": len(dirs), "h": h, "max_rel_err": max(errs) if errs else None,
                          "median_rel_err": statistics.median(errs) if errs else None},
             "descent": {"iterations": args.adjoint_iters, "accepted": len(hist) - 1, "J_first": hist[0],
@@ -556,6 +565,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
+    ap.add_argument("--save-tiles", default=None)
     ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
     ap.add_argument("--adjoint-horizon", type=int, default=200)
     ap.add_argument("--adjoint-fd", type=int, default=20, help="finite-difference directions")

@@ -676,7 +676,7 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     for ctas in (1, 2, 3, 4):
         tb = (SMEM_PER_SM // ctas - 2048) // per_line
         tbs.add(int(tb))
-    tbs.update({4, 8, 16})
+    tbs.update({1, 2, 4, 8, 16})
     out = []
     for tb in sorted(tbs):
         tb = min(tb, 64, max(max_lines, 1))
@@ -721,79 +721,109 @@ class FusedBatch:
         self._build_launches()
         self.graph = None
 
-    def _pass_geometry(self, prog):
-        lines = [I.lines(prog) for I in self.insts]
-        maxlen = max(program_maxlen(prog, I.lens) for I in self.insts)
-        lcap = (maxlen + 1) | 1
-        fft_n = max(I.lens[L_ND + prog.axis] for I in self.insts) if (prog.has_dct and self.fft) else 0
-        return lines, lcap, fft_n
+    # ------------------------------------------------------------- launches
+    # A pass over a heterogeneous batch is split into one launch per class of
+    # instances with the same slot capacity (longest line) and FFT length: the
+    # shared-memory tile of a launch is sized for its own class, so a launch of
+    # small instances holds proportionally more lines per CTA instead of
+    # padding every line to the largest instance's length.
+    def _groups(self, prog):
+        """[((lcap, fft_n), [instance indices])] for one pass, largest class first."""
+        g = {}
+        for k, I in enumerate(self.insts):
+            lcap = (program_maxlen(prog, I.lens) + 1) | 1
+            fft_n = I.lens[L_ND + prog.axis] if (prog.has_dct and self.fft) else 0
+            g.setdefault((lcap, fft_n), []).append(k)
+        return sorted(g.items(), reverse=True)
 
-    def _launch(self, prog, tb, nt, d_insts=None):
-        dev = device()
-        lines, lcap, fft_n = self._pass_geometry(prog)
+    def _d_insts(self, prog):
+        insts = (_lib.PgxInstance * len(self.insts))()
+        for k, I in enumerate(self.insts):
+            I.fill(prog, insts[k])
+        return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
+
+    def _group_launch(self, prog, d_insts, key, members, tb, nt):
+        lcap, fft_n = key
         P = _lib.PgxProgram()
         P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
         P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
         assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
         for i, o in enumerate(prog.ops):
             P.ops[i] = o
-        if d_insts is None:
-            insts = (_lib.PgxInstance * len(self.insts))()
-            for k, I in enumerate(self.insts):
-                I.fill(prog, insts[k])
-            d_insts = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(dev)
-        work = []
-        for k, nl in enumerate(lines):
-            work += [(k, t) for t in range(-(-nl // tb))]
-        d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=dev)
-        return (prog.name, P, d_insts, d_work, len(work))
+        work = [(k, t) for k in members for t in range(-(-self.insts[k].lines(prog) // tb))]
+        d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
+        return {"name": prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
+                "key": key, "members": members, "prog": prog}
+
+    def _pass_launches(self, prog, tiles=None, index=None):
+        d_insts = self._d_insts(prog)
+        out = []
+        for gi, (key, members) in enumerate(self._groups(prog)):
+            lines = [self.insts[k].lines(prog) for k in members]
+            tag = "%s#%d" % (prog.name, gi)
+            if tiles and tag in tiles:
+                tb, nt = tiles[tag][:2]
+            else:
+                tb, nt = _pick(prog, sum(lines), key[0], key[1], max(lines))
+            out.append(self._group_launch(prog, d_insts, key, members, tb, nt))
+        return out
 
     def _build_launches(self, tiles=None):
-        """Launch descriptors of the forward passes; ``tiles`` = {pass: (lines per CTA, threads)}
-        overrides the default choice (e.g. another batch's autotuned tiles)."""
-        self.launches = []
-        for prog in self.progs:
-            lines, lcap, fft_n = self._pass_geometry(prog)
-            if tiles and prog.name in tiles:
-                tb, nt = tiles[prog.name][:2]
-            else:
-                tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
-            self.launches.append(self._launch(prog, tb, nt))
+        """Launch descriptors of the forward passes; ``tiles`` = {"pass#group": (lines per CTA,
+        threads)} overrides the default choice (e.g. another batch's autotuned tiles)."""
+        self.launches = [self._pass_launches(p, tiles) for p in self.progs]
+
+    @staticmethod
+    def _tiles_of(launch_sets):
+        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads)
+                for group in launch_sets for gi, L in enumerate(group)}
 
     def tiles(self):
-        """{pass: (lines per CTA, threads)} of the current launches."""
-        return {L[0]: (L[1].tb, L[1].nthreads) for L in self.launches}
+        """{"pass#group": (lines per CTA, threads)} of the current forward launches."""
+        return self._tiles_of(self.launches)
 
-    def autotune(self, reps=3, verbose=False):
-        """Time every candidate tile shape of every pass on this batch and keep the fastest.
+    def _run_launch(self, L):
+        _lib.check(_lib.lib().pgx_run_batched(ctypes.byref(L["P"]), L["d_insts"].data_ptr(), L["d_work"].data_ptr(),
+                                              L["nwork"], stream()), L["name"])
 
-        The passes update the state in place, so the state is saved before and
-        restored after tuning.  Returns {pass: (lines per CTA, threads, ms)}.
-        """
-        saved = [{k: I.arrays[k].clone() for k in _Instance.STATE} for I in self.insts]
+    def run_pass(self, i):
+        for L in self.launches[i]:
+            self._run_launch(L)
+
+    def _tune(self, launch_sets, reps, verbose):
+        """Time every candidate tile of every launch (each alone) and keep the fastest.
+        The caller saves and restores whatever state the launches modify."""
         stream = torch.cuda.current_stream()
         chosen = {}
-        for i, prog in enumerate(self.progs):
-            lines, lcap, fft_n = self._pass_geometry(prog)
-            best = None
-            d_insts = self.launches[i][2]
-            for tb, nt in _candidates(prog, sum(lines), lcap, fft_n, max(lines)):
-                L = self._launch(prog, tb, nt, d_insts)
-                self.launches[i] = L
-                self.run_pass(i)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for _ in range(reps):
-                    self.run_pass(i)
-                b.record(stream)
-                torch.cuda.synchronize()
-                ms = a.elapsed_time(b) / reps
-                if verbose:
-                    print(prog.name, tb, nt, round(ms, 4))
-                if best is None or ms < best[0]:
-                    best = (ms, L, tb, nt)
-            self.launches[i] = best[1]
-            chosen[prog.name] = (best[2], best[3], round(best[0], 4))
+        for group in launch_sets:
+            for gi, L0 in enumerate(group):
+                prog, key, members = L0["prog"], L0["key"], L0["members"]
+                lines = [self.insts[k].lines(prog) for k in members]
+                best = None
+                for tb, nt in _candidates(prog, sum(lines), key[0], key[1], max(lines)):
+                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt)
+                    self._run_launch(L)
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    for _ in range(reps):
+                        self._run_launch(L)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    ms = a.elapsed_time(b) / reps
+                    if verbose:
+                        print(prog.name, gi, tb, nt, round(ms, 4))
+                    if best is None or ms < best[0]:
+                        best = (ms, L, tb, nt)
+                group[gi] = best[1]
+                chosen["%s#%d" % (prog.name, gi)] = (best[2], best[3], round(best[0], 4))
+        return chosen
+
+    def autotune(self, reps=3, verbose=False):
+        """Time every candidate tile shape of every launch of every pass on this batch and keep
+        the fastest.  The passes update the state in place, so the state is saved before and
+        restored after tuning.  Returns {"pass#group": (lines per CTA, threads, ms)}."""
+        saved = [{k: I.arrays[k].clone() for k in _Instance.STATE} for I in self.insts]
+        chosen = self._tune(self.launches, reps, verbose)
         for I, s in zip(self.insts, saved):
             for k, v in s.items():
                 I.arrays[k].copy_(v)
@@ -801,11 +831,6 @@ class FusedBatch:
         self.graph = None
         self.tuned = chosen
         return chosen
-
-    def run_pass(self, i):
-        name, P, d_insts, d_work, nwork = self.launches[i]
-        _lib.check(_lib.lib().pgx_run_batched(ctypes.byref(P), d_insts.data_ptr(), d_work.data_ptr(), nwork,
-                                              stream()), name)
 
     def step_eager(self):
         for i in range(len(self.launches)):
@@ -840,7 +865,7 @@ class FusedBatch:
 
     @property
     def launches_per_step(self):
-        return len(self.launches)
+        return sum(len(g) for g in self.launches)
 
     def single(self, i):
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""

@@ -39,7 +39,7 @@ import torch
 from .. import _lib
 from .._dev import DTYPE, device, to_dev
 from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX, P_MDTSZ,
-                    P_MNU, FusedBatch, Prog, _candidates, _Instance, _pick, build_programs, host_tables)
+                    P_MNU, FusedBatch, Prog, _Instance, build_programs, host_tables)
 
 BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
@@ -334,20 +334,12 @@ class FusedAdjoint(FusedBatch):
             add_adjoint_buffers(I, views)
         tkind = self.solvers[0].T.xs[0].id
         self.aprogs = build_adjoint_programs(tkind, self.fft)
-        self.alaunches = [self._default_launch(p) for p in self.aprogs]
+        self.alaunches = [self._pass_launches(p) for p in self.aprogs]
         self.agraph = None
 
-    def _default_launch(self, prog):
-        lines, lcap, fft_n = self._pass_geometry(prog)
-        tb, nt = _pick(prog, sum(lines), lcap, fft_n, max(lines))
-        return self._launch(prog, tb, nt)
-
     def run_adjoint_pass(self, i):
-        name, P, d_insts, d_work, nwork = self.alaunches[i]
-        import ctypes
-        from .._dev import stream
-        _lib.check(_lib.lib().pgx_run_batched(ctypes.byref(P), d_insts.data_ptr(), d_work.data_ptr(), nwork,
-                                              stream()), name)
+        for L in self.alaunches[i]:
+            self._run_launch(L)
 
     def adjoint_step_eager(self):
         for i in range(len(self.alaunches)):
@@ -359,32 +351,14 @@ class FusedAdjoint(FusedBatch):
         else:
             self.adjoint_step_eager()
 
+    @property
+    def adjoint_launches_per_step(self):
+        return sum(len(g) for g in self.alaunches)
+
     def autotune_adjoint(self, reps=3, verbose=False):
-        """Per-pass tile choice for the adjoint passes (state and gradients restored after)."""
+        """Tile choice for every launch of the adjoint passes (state and gradients restored after)."""
         saved_s, saved_b = self.state_arena.clone(), self.bar_arena.clone()
-        stream = torch.cuda.current_stream()
-        chosen = {}
-        for i, prog in enumerate(self.aprogs):
-            lines, lcap, fft_n = self._pass_geometry(prog)
-            d_insts = self.alaunches[i][2]
-            best = None
-            for tb, nt in _candidates(prog, sum(lines), lcap, fft_n, max(lines)):
-                L = self._launch(prog, tb, nt, d_insts)
-                self.alaunches[i] = L
-                self.run_adjoint_pass(i)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for _ in range(reps):
-                    self.run_adjoint_pass(i)
-                b.record(stream)
-                torch.cuda.synchronize()
-                ms = a.elapsed_time(b) / reps
-                if verbose:
-                    print(prog.name, tb, nt, round(ms, 4))
-                if best is None or ms < best[0]:
-                    best = (ms, L, tb, nt)
-            self.alaunches[i] = best[1]
-            chosen[prog.name] = (best[2], best[3], round(best[0], 4))
+        chosen = self._tune(self.alaunches, reps, verbose)
         self.state_arena.copy_(saved_s)
         self.bar_arena.copy_(saved_b)
         torch.cuda.synchronize()
