@@ -36,6 +36,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "2D RBC FP64 steps/s at 1 GB300: plain vs batched-graph; adjoint grads/s at 1e-6 rel"
 FP64_PEAK_TFLOPS = 1.19  # measured DFMA throughput of this GB300 (profiles/gb300_fp64_probe.txt)
+# DRAM bytes (read + write) of pass P2 on the 256-instance workload, one ncu capture of its three size-class
+# launches (profiles/line_program_batched_c4_launches.txt)
+P2_DRAM_BYTES = 154.5e6 + 37.6e6
 
 
 def workload_specs(kind, n_instances, rank=0):
@@ -315,7 +318,8 @@ def run_gpu(args, rank, world):
     achieved = fl_dom / (pt[dom] * 1e-3) / 1e12
     roofline = {"bound": "fp64", "kernel": "line_program_batched (%s)" % work[dom][0], "achieved": round(achieved, 4),
                 "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4),
-                "traffic": None,
+                "traffic": P2_DRAM_BYTES if (work[dom][0] == "P2" and args.workload == "c4" and n_inst == 256)
+                else None,
                 "peak_source": "measured DFMA peak of this GB300 (profiles/gb300_fp64_probe.txt); the "
                                "driver-written peak file carries only HBM and bf16",
                 "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2]}
