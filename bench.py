@@ -63,6 +63,22 @@ WORKLOAD_NAMES = {
 }
 
 
+def max_over_ranks(x):
+    """Max of a host scalar over the ranks of the default process group (nccl: through the
+    rank's GPU; gloo: on the host)."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_value(n_inst_per_rank, world, steps, total_ms_max):
+    """Whole-job instance-steps/s: every rank steps its own instances; time = the slowest rank."""
+    return n_inst_per_rank * world * steps / (total_ms_max / 1e3)
+
+
 # ------------------------------------------------------------------ CPU side
 _WORKER = {}
 BLAS_ENV = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
@@ -230,10 +246,13 @@ def run_gpu(args, rank, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         sample = specs[::8] if args.workload == "c4" else specs
-        steps_cpu = 1 if args.workload == "c4" else (20 if args.workload == "c1" else 1)
         ncores = min(cores, len(sample))
         port = CpuPort(sample, ncores)
-        done, wall = port.step(steps_cpu)
+        port.step(1)  # warm-up (first-step caches, BLAS initialisation)
+        done, wall, steps_cpu = 0, 0.0, 0
+        while wall < 10.0 and steps_cpu < 1000:  # a bounded sample: about 10 s of stepping
+            d, w = port.step(1)
+            done, wall, steps_cpu = done + d, wall + w, steps_cpu + 1
         port.close()
         cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port",
                "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (NumPy "
@@ -274,10 +293,8 @@ def run_gpu(args, rank, world):
     clk = clocks.stop()
     total_ms = sum(step_ms)
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = n_inst * world * args.steps / (total_ms / 1e3)
+        total_ms = max_over_ranks(total_ms)
+    value = aggregate_value(n_inst, world, args.steps, total_ms)
     finite = int(sum(bool(torch.isfinite(I.arrays["TG"]).all()) for I in fb.insts))
 
     # e2e: public API, state in pinned host memory, H2D before and D2H after every step
@@ -295,9 +312,7 @@ def run_gpu(args, rank, world):
     e2e_ms = time_steps(e2e_step, args.steps, stream)
     e2e_total = sum(e2e_ms)
     if world > 1:
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+        e2e_total = max_over_ranks(e2e_total)
     e2e = {"value": n_inst * world * args.steps / (e2e_total / 1e3), "unit": "instance-steps/s",
            "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}
 

@@ -493,6 +493,9 @@ def instance_params(N, M, dealias, dt, nu, kappa, scale):
     return lens, par
 
 
+A_KEYS = ("A_U0", "A_Ux", "A_V0", "A_Vx", "A_T0", "A_Tx")
+
+
 def scratch_shapes(N, M, Nd, Md):
     """Intermediate arrays of the forward passes (name -> shape)."""
     sh = {}
@@ -547,7 +550,7 @@ class _Instance:
         a["DTB1"] = ns.dTbcdz1.contiguous()
         a["DTB2"] = ns.dTbcdz2.contiguous()
         for k, shp in scratch_shapes(N, M, Nd, Md).items():
-            a[k] = z(*shp)
+            a[k] = views[k] if (views is not None and k in views) else z(*shp)
         self.arrays = a
         self.lens, self.par = instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale)
         # operator tables
@@ -709,13 +712,22 @@ class FusedBatch:
         shapes = [_Instance.state_shapes(ns) for ns in self.solvers]
         total = sum(r * c for sh in shapes for (r, c) in sh.values())
         self.state_arena = torch.zeros(total, dtype=DTYPE, device=device())
-        self.insts, off = [], 0
-        for ns, sh in zip(self.solvers, shapes):
+        # the physical-space operands of the convection terms (pass P1's outputs) of all instances
+        # share a second arena: the reverse sweep keeps them per step with one copy per batch
+        ashapes = [{k: v for k, v in scratch_shapes(*ns.shape, *nd).items() if k in A_KEYS}
+                   for ns, nd in zip(self.solvers, sizes)]
+        self.a_arena = torch.zeros(sum(r * c for sh in ashapes for (r, c) in sh.values()), dtype=DTYPE,
+                                   device=device())
+        self.insts, off, aoff = [], 0, 0
+        for ns, sh, ash in zip(self.solvers, shapes, ashapes):
             views = {}
             for key in _Instance.STATE:
                 r, c = sh[key]
                 views[key] = self.state_arena[off:off + r * c].view(r, c)
                 off += r * c
+            for key, (r, c) in ash.items():
+                views[key] = self.a_arena[aoff:aoff + r * c].view(r, c)
+                aoff += r * c
             self.insts.append(_Instance(ns, self.fft, views, bind))
         self.progs = build_programs(tkinds.pop(), self.fft)
         self._build_launches()

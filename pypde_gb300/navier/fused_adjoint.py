@@ -341,8 +341,10 @@ class FusedAdjoint(FusedBatch):
         for L in self.alaunches[i]:
             self._run_launch(L)
 
-    def adjoint_step_eager(self):
-        for i in range(len(self.alaunches)):
+    def adjoint_step_eager(self, recompute=True):
+        """The reverse-mode passes; ``recompute=False`` skips R1 when the caller has put the
+        step's P1 outputs (``a_arena``) in place itself."""
+        for i in range(0 if recompute else 1, len(self.alaunches)):
             self.run_adjoint_pass(i)
 
     def adjoint_step(self):
@@ -399,8 +401,9 @@ class HorizonGradient:
 
     Forward states are checkpointed every ``every`` steps during the forward
     sweep.  The reverse sweep recomputes each segment from its checkpoint
-    (``every`` fused steps, states kept in a trajectory buffer) and steps it
-    back with the adjoint passes.  With ``overlap`` the recomputation of
+    (``every`` fused steps; what the adjoint passes read of each step, the P1
+    outputs, is kept in a trajectory buffer) and steps it back with the
+    adjoint passes.  With ``overlap`` the recomputation of
     segment s-1 runs on a second stream, on a private working copy of the
     batch, while the adjoint passes of segment s run on the main stream (two
     trajectory buffers alternate); a single small instance leaves most SMs
@@ -417,7 +420,9 @@ class HorizonGradient:
         dev = fa.state_arena.device
         z = lambda *shape: torch.zeros(shape, dtype=DTYPE, device=dev)  # noqa: E731
         self.ckpt = z(self.nseg, n)
-        self.traj = z(2 if overlap else 1, every, n)
+        # per step of a segment: the P1 outputs (physical-space operands of the convection terms),
+        # which is all the reverse-mode passes read of the forward state
+        self.traj = z(2 if overlap else 1, every, fa.a_arena.numel())
         self.x0, self.x_in, self.g_out = z(n), z(n), z(n)
         self.J_out = z(len(fa.insts))
         self._mask = z(n)
@@ -456,19 +461,21 @@ class HorizonGradient:
         return J, r * scale
 
     def _recompute(self, batch, s, buf):
-        """States at the start of every step of segment s into traj[buf] (batch: a working set)."""
+        """P1 outputs of every step of segment s into traj[buf] (batch: a working set)."""
         k = self._seg_len(s)
         batch.state_arena.copy_(self.ckpt[s])
         for j in range(k):
-            self.traj[buf, j].copy_(batch.state_arena)
             if j + 1 < k:
                 batch.step_eager()
+            else:
+                batch.run_pass(0)           # the last step only needs its P1
+            self.traj[buf, j].copy_(batch.a_arena)
 
     def _reverse(self, s, buf):
         fa = self.fa
         for j in reversed(range(self._seg_len(s))):
-            fa.state_arena.copy_(self.traj[buf, j])
-            fa.adjoint_step_eager()
+            fa.a_arena.copy_(self.traj[buf, j])
+            fa.adjoint_step_eager(recompute=False)
 
     def _reverse_sweep(self):
         if not self.overlap:

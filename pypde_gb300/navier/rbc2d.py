@@ -15,6 +15,7 @@ from ..field import Field, FieldBC, MultiField
 from ..field_operations import avg_vol, avg_x, cheby_to_galerkin, convective_term, galerkin_to_cheby, grad
 from ..solver import Integrator
 from ..templates import solverplan_hholtz2d_adi, solverplan_poisson2d
+from .steady import NavierStokesSteadyState
 
 CONFIG = {"shape": (50, 50), "ra": 5e3, "pr": 1.0, "dt": 0.2, "ndim": 2, "tsave": 0.1, "dealias": True,
           "integrator": "eu", "beta": 1.0, "aspect": 1.0}
@@ -112,7 +113,7 @@ def eval_Nuvol(T, V, kappa, field, Lz=1.0, Tbc=None):
     return float(avg_vol((Tv * Vv / kappa - dT) * Lz, field.dx, field.dy))
 
 
-class NavierStokes(NavierStokesBase, Integrator):
+class NavierStokes(NavierStokesBase, NavierStokesSteadyState, Integrator):
     """Boussinesq convection, IMEX Euler / RK3 with pressure projection (rbc2d.py:28-434)."""
 
     avail_cases = ["rbc", "linear", "zero"]
