@@ -472,6 +472,30 @@ def run_adjoint(args, stream):
         fd = (float(hg.value(X + h * D)[0]) - float(hg.value(X - h * D)[0])) / (2 * h)
         ad = float((g * D).sum())
         errs.append(abs(fd - ad) / abs(ad))
+    # many searches at once: a batch of instances of the same configuration (noise seeds 3, 4, ...)
+    batched = None
+    if args.adjoint_batch > 1:
+        solvers = []
+        for i in range(args.adjoint_batch):
+            nsi = NavierStokes(case="linear", shape=shape, ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu",
+                               tsave=None)
+            nsi.set_temperature_noise(3 + i, 1e-2)
+            solvers.append(nsi)
+        fab = FusedAdjoint(solvers)
+        if not args.no_tune:
+            fab.autotune(reps=2)
+            fab.autotune_adjoint(reps=2)
+        hgb = HorizonGradient(fab, H, every)
+        Xb = fab.state_arena.clone()
+        for _ in range(2):
+            hgb.value_and_grad(Xb)
+        torch.cuda.synchronize()
+        ms_b, (Jb, gb) = timed(lambda: hgb.value_and_grad(Xb), 2)
+        batched = {"instances": args.adjoint_batch, "ms_per_batch_grad": round(ms_b, 3),
+                   "grads_per_s": round(args.adjoint_batch * 1e3 / ms_b, 3),
+                   "finite": bool(torch.isfinite(gb).all())}
+        del hgb, fab, solvers
+        torch.cuda.empty_cache()
     # steady-state search: descent iterations, one gradient evaluation each
     t0 = time.perf_counter()
     _, hist = descend(hg.value_and_grad, X, args.adjoint_iters)
@@ -490,6 +514,7 @@ def run_adjoint(args, stream):
             "descent": {"iterations": args.adjoint_iters, "accepted": len(hist) - 1, "J_first": hist[0],
                         "J_last": hist[-1], "wall_s": round(wall_desc, 3),
                         "step": "alpha J / |grad J|^2, alpha adapted by acceptance"},
+            "batched": batched,
             "J": float(J[0]), "autotuned_adjoint_tiles": getattr(fa, "atuned", None)}
 
 
@@ -590,6 +615,7 @@ def main():
     ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
     ap.add_argument("--adjoint-horizon", type=int, default=200)
     ap.add_argument("--adjoint-fd", type=int, default=20, help="finite-difference directions")
+    ap.add_argument("--adjoint-batch", type=int, default=32, help="instances of the batched gradient measurement")
     ap.add_argument("--adjoint-profile", type=int, default=0,
                     help="c5 only: run N eager forward and N adjoint steps (fixed launch order) and exit")
     args = ap.parse_args()
