@@ -407,7 +407,7 @@ def run_gpu(args, rank, world):
         line["clocks"] = clk
     if cpu:
         line["cpu_baseline"] = cpu
-    if world == 1 and args.adjoint_iters >= 0:
+    if world == 1 and args.adjoint_iters >= 0 and args.workload == "c4":
         line["adjoint"] = run_adjoint(args, stream)
     return line
 

@@ -429,7 +429,7 @@ static int cheb_diff_op(int code, const double* c, int64_t c_s0, int64_t c_s1, d
 struct pgx_stencil_plan {
   int N;
   double* sub;    // S[i+2, i], i < N-2 (length N)
-  double* tdma;   // offset-2 TDMA factors, interleaved (a, rden, w) per index
+  double* tdma;   // offset-2 TDMA factors, interleaved (a r, r, w) per index (r: reciprocal pivot)
 };
 struct pgx_tdma_plan {
   int n;
@@ -437,7 +437,9 @@ struct pgx_tdma_plan {
 };
 
 // Offset-2 TDMA table from diagonals a (n-2, offset -2), b (n), c (n-2, offset +2),
-// interleaved per index i: (a_{i-2}, 1/(b_i - a_{i-2} w_{i-2}), w_i).
+// interleaved per index i: (a_{i-2} r_i, r_i, w_i) with the reciprocal pivot
+// r_i = 1/(b_i - a_{i-2} w_{i-2}); the forward sweep g_i = r_i x_i - (a_{i-2} r_i) g_{i-2}
+// then has one dependent FMA per step.
 static int tdma_table(const double* a, const double* b, const double* c, int n, std::vector<double>& tab) {
   tab.assign(3 * (size_t)n, 0.0);
   std::vector<double> w(n, 0.0);
@@ -445,7 +447,7 @@ static int tdma_table(const double* a, const double* b, const double* c, int n, 
     double den = i < 2 ? b[i] : b[i] - a[i - 2] * w[i - 2];
     if (den == 0.0) return PGX_E_SINGULAR;
     if (i < n - 2) w[i] = c[i] / den;
-    tab[3 * i] = i < 2 ? 0.0 : a[i - 2];
+    tab[3 * i] = i < 2 ? 0.0 : a[i - 2] / den;
     tab[3 * i + 1] = 1.0 / den;
     tab[3 * i + 2] = w[i];
   }
@@ -628,7 +630,7 @@ extern "C" int pgx_tdma_solve(const pgx_tdma_plan* p, const double* d, int64_t d
 // ------------------------------------------------------------------ FDMA
 struct pgx_fdma_plan {
   int n;
-  double* tab;  // [l | dinv | u1 | u2]
+  double* tab;  // [l | dinv | u1 dinv | u2 dinv]
 };
 
 static void fdma_tab(const double* l, const double* d, const double* u1, const double* u2, int n,
@@ -636,8 +638,8 @@ static void fdma_tab(const double* l, const double* d, const double* u1, const d
   for (int i = 0; i < n; ++i) {
     tab[off + i] = (i >= 2 && l) ? l[i - 2] : 0.0;
     tab[off + n + i] = 1.0 / d[i];
-    tab[off + 2 * n + i] = (i < n - 2 && u1) ? u1[i] : 0.0;
-    tab[off + 3 * n + i] = (i < n - 4 && u2) ? u2[i] : 0.0;
+    tab[off + 2 * n + i] = (i < n - 2 && u1) ? u1[i] / d[i] : 0.0;
+    tab[off + 3 * n + i] = (i < n - 4 && u2) ? u2[i] / d[i] : 0.0;
   }
 }
 
@@ -705,7 +707,7 @@ static int fdma_solve_op(int code, const pgx_fdma_plan* p, double* x, int64_t s0
 // ---------------------------------------------------------------- Poisson
 struct pgx_poisson_plan {
   int n, m;
-  double* tab;  // m lines x [l | dinv | u1 | u2] (n each)
+  double* tab;  // m lines x [l | dinv | u1 dinv | u2 dinv] (n each)
 };
 
 // LU sweep of the four diagonals of an n x n band (init_fdma's recurrence).
@@ -747,8 +749,8 @@ extern "C" int pgx_poisson_plan_create(const double* A, const double* C, const d
       int g = i + o;
       tab[base + g] = i >= 2 ? l[i - 2] : 0.0;
       tab[base + n + g] = 1.0 / d[i];
-      tab[base + 2 * n + g] = i < ns - 2 ? u1[i] : 0.0;
-      tab[base + 3 * n + g] = i < ns - 4 ? u2[i] : 0.0;
+      tab[base + 2 * n + g] = i < ns - 2 ? u1[i] / d[i] : 0.0;
+      tab[base + 3 * n + g] = i < ns - 4 ? u2[i] / d[i] : 0.0;
     }
   }
   pgx_poisson_plan* p = new pgx_poisson_plan();

@@ -259,8 +259,8 @@ __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     double* x = slot_ptr(c, op.a + s) + t * c.lcap;
     double g = 0.0;
     int i = p;
-    for (; i < n; i += 2) {
-      g = (x[i] - __ldg(tab + 3 * i) * g) * __ldg(tab + 3 * i + 1);
+    for (; i < n; i += 2) {  // g_i = r_i x_i - (a r)_i g_{i-2}: one dependent FMA per step
+      g = fma(-__ldg(tab + 3 * i), g, x[i] * __ldg(tab + 3 * i + 1));
       x[i] = g;
     }
     double xn = 0.0;
@@ -370,9 +370,9 @@ __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, 
     x[i] = prev;
   }
   double x2 = 0.0, x4 = 0.0;
-  for (i -= 2; i >= 0; i -= 2) {
-    double v = fma(-__ldg(u2 + i), x4, x[i]);
-    v = fma(-__ldg(u1 + i), x2, v) * __ldg(dinv + i);
+  for (i -= 2; i >= 0; i -= 2) {  // u1, u2 hold u dinv: one FMA on the x2 dependency
+    const double w = fma(-__ldg(u2 + i), x4, x[i] * __ldg(dinv + i));
+    const double v = fma(-__ldg(u1 + i), x2, w);
     x[i] = v;
     x4 = x2;
     x2 = v;
@@ -382,21 +382,21 @@ __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, 
 // FDMA over ns slots: slot a+s uses factor table mat+s.  POISSON (per_line):
 // single table with per-line factors.
 // Transposed solve A^T x = b with the factors of A = L U (adjoint of fdma_chain):
-//   U^T z = b (forward):  z_i = (b_i - u1_{i-2} z_{i-2} - u2_{i-4} z_{i-4}) dinv_i
+//   U^T z = b (forward):  z_i = (b_i - u1_{i-2} z_{i-2} - u2_{i-4} z_{i-4}) dinv_i, run on
+//                         zeta_i = z_i / dinv_i = b_i - (u1 dinv)_{i-2} zeta_{i-2} - (u2 dinv)_{i-4} zeta_{i-4}
 //   L^T x = z (backward): x_i = z_i - l_{i+2} x_{i+2}
 __device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n, int p) {
   const double* l = tab;
   const double* dinv = tab + n;
-  const double* u1 = tab + 2 * n;
-  const double* u2 = tab + 3 * n;
-  double z2 = 0.0, z4 = 0.0;
+  const double* u1 = tab + 2 * n;  // u1 dinv
+  const double* u2 = tab + 3 * n;  // u2 dinv
+  double z2 = 0.0, z4 = 0.0;       // zeta_{i-2}, zeta_{i-4}
   int i = p;
   for (; i < n; i += 2) {
     double v = x[i];
     if (i >= 4) v = fma(-__ldg(u2 + i - 4), z4, v);
     if (i >= 2) v = fma(-__ldg(u1 + i - 2), z2, v);
-    v *= __ldg(dinv + i);
-    x[i] = v;
+    x[i] = v * __ldg(dinv + i);
     z4 = z2;
     z2 = v;
   }

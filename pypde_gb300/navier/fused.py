@@ -364,7 +364,8 @@ def global_tables_host():
             den = b[i] if i < 2 else b[i] - a[i - 2] * w[i - 2]
             w[i] = c[i] / den
             rden[i] = 1.0 / den
-            aa[i] = 0.0 if i < 2 else a[i - 2]
+            aa[i] = 0.0 if i < 2 else a[i - 2] / den
+        # interleaved (a r, r, w): the forward sweep g_i = r_i x_i - (a r)_i g_{i-2}
         t["tdma_" + kind] = np.stack([aa, rden, w], axis=1).ravel()
     return t
 
@@ -397,19 +398,21 @@ def _banded_table(A, off0, ndiag):
 
 
 def _fdma_table(A):
+    """[l | 1/d | u1/d | u2/d]: the upper factor pre-scaled so each back-substitution step is
+    one FMA on the dependency chain."""
     l, d, u1, u2 = fdma_lu(A)
     n = d.size
     tab = np.zeros((4, n))
     tab[0, 2:] = l
     tab[1] = 1.0 / d
-    tab[2, :n - 2] = u1
-    tab[3, :n - 4] = u2
+    tab[2, :n - 2] = u1 / d[:n - 2]
+    tab[3, :n - 4] = u2 / d[:n - 4]
     return tab.ravel()
 
 
 def _poisson_table(Ax, Cx, lam):
     """Per-eigenvalue LU factors of A + lam_j C with the singular rule (fdma.f90:146-185),
-    laid out [l | dinv | u1 | u2] per line; a singular line solves rows 1: and has dinv_0 = 0."""
+    laid out [l | 1/d | u1/d | u2/d] per line; a singular line solves rows 1: and has 1/d_0 = 0."""
     n = Ax.shape[0]
     m = lam.size
     tab = np.zeros((m, 4, n))
@@ -420,8 +423,8 @@ def _poisson_table(Ax, Cx, lam):
         ns = n - o
         tab[j, 0, o + 2:] = l
         tab[j, 1, o:] = 1.0 / d
-        tab[j, 2, o:o + ns - 2] = u1
-        tab[j, 3, o:o + ns - 4] = u2
+        tab[j, 2, o:o + ns - 2] = u1 / d[:ns - 2]
+        tab[j, 3, o:o + ns - 4] = u2 / d[:ns - 4]
     return tab.ravel()
 
 

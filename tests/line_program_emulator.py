@@ -36,7 +36,8 @@ def cheb_diff_matrix(n):
 
 
 def _fdma(x, tab, n, transpose):
-    l, dinv, u1, u2 = tab[:n], tab[n:2 * n], tab[2 * n:3 * n], tab[3 * n:4 * n]
+    """Banded LU sweep with the device table [l | 1/d | u1/d | u2/d] (per parity chain)."""
+    l, dinv, u1d, u2d = tab[:n], tab[n:2 * n], tab[2 * n:3 * n], tab[3 * n:4 * n]
     for p in (0, 1):
         idx = list(range(p, n, 2))
         if not transpose:
@@ -44,19 +45,18 @@ def _fdma(x, tab, n, transpose):
                 x[i] -= l[i] * x[i - 2]
             x2 = x4 = 0.0
             for i in reversed(idx):
-                v = (x[i] - u2[i] * x4 - u1[i] * x2) * dinv[i]
+                v = x[i] * dinv[i] - u2d[i] * x4 - u1d[i] * x2
                 x[i] = v
                 x4, x2 = x2, v
         else:
-            z2 = z4 = 0.0
+            z2 = z4 = 0.0   # zeta = z / dinv
             for i in idx:
                 v = x[i]
                 if i >= 4:
-                    v -= u2[i - 4] * z4
+                    v -= u2d[i - 4] * z4
                 if i >= 2:
-                    v -= u1[i - 2] * z2
-                v *= dinv[i]
-                x[i] = v
+                    v -= u1d[i - 2] * z2
+                x[i] = v * dinv[i]
                 z4, z2 = z2, v
             xn = 0.0
             for i in reversed(idx):

@@ -82,3 +82,35 @@ def test_adjoint_programs_are_the_transposed_step(N, M, tk, dealias, fft):
     rhs = sum(float((m.arrays["b" + k] * d[k]).sum()) for k in STATE)
     scale = sum(float(np.abs(g[k] * jd[k]).sum()) for k in STATE)
     assert abs(lhs - rhs) <= 1e-9 * scale, (lhs, rhs)
+
+
+def test_banded_tables_solve_and_transpose():
+    """The device factor tables (emulated sweeps) solve A x = b and A^T x = b, incl. a singular
+    Poisson line (row and column 0 dropped, x_0 = 0)."""
+    from line_program_emulator import _fdma
+    from pypde_gb300.navier.fused import _fdma_table, _poisson_table
+    rng = np.random.default_rng(3)
+    n = 21
+    Bx = pseudoinverse_d2(n + 2)[2:, :]
+    S = stencil_matrix("CD", n + 2)
+    A = Bx @ S - 0.03 * np.eye(n + 2)[2:, :] @ S
+    b = rng.standard_normal(n)
+    for transpose, M in ((False, A), (True, A.T)):
+        x = b.copy()
+        _fdma(x, _fdma_table(A), n, transpose)
+        assert np.allclose(M @ x, b, rtol=0, atol=1e-12 * np.abs(b).max())
+    Sn = stencil_matrix("CN", n + 2)
+    Ax, Cx = np.eye(n + 2)[2:, :] @ Sn, pseudoinverse_d2(n + 2)[2:, :] @ Sn
+    lam = np.array([0.0, -3.0])
+    tab = _poisson_table(Ax, Cx, lam)
+    for j, lj in enumerate(lam):
+        K = Ax + lj * Cx
+        for transpose in (False, True):
+            x = b.copy()
+            _fdma(x, tab[j * 4 * n:(j + 1) * 4 * n], n, transpose)
+            if abs(lj) < 1e-10:
+                ref = np.zeros(n)
+                ref[1:] = np.linalg.solve((K.T if transpose else K)[1:, 1:], b[1:])
+            else:
+                ref = np.linalg.solve(K.T if transpose else K, b)
+            assert np.allclose(x, ref, rtol=0, atol=1e-10 * np.abs(ref).max()), (j, transpose)
