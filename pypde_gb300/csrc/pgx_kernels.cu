@@ -358,6 +358,12 @@ __device__ void op_diff_t(Ctx& c, const pgx_op& op) {
 // In-place banded LU sweep for offsets -2, 0, +2, +4 (fdma.f90:1-38) with
 // factors [l | dinv | u1 | u2] (each n, zero-padded, l[i] couples x_i to x_{i-2}):
 //   forward  x_i -= l_i x_{i-2};   backward x_i = (x_i - u1_i x_{i+2} - u2_i x_{i+4}) dinv_i
+// A chain step waits for its factor loads; the per-line Poisson factors are touched once,
+// so they would come from L2 at every step.  Each step therefore asks L1 for the factors
+// PF elements ahead (in-bounds addresses only; a prefetch is a hint and changes no result).
+constexpr int PF = 32;
+__device__ __forceinline__ void prefetch_l1(const double* a) { asm volatile("prefetch.L1 [%0];" ::"l"(a)); }
+
 __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, int p) {
   const double* l = tab;
   const double* dinv = tab + n;
@@ -366,11 +372,17 @@ __device__ __forceinline__ void fdma_chain(double* x, const double* tab, int n, 
   double prev = x[p];
   int i = p + 2;
   for (; i < n; i += 2) {
+    if (i + PF < n) prefetch_l1(l + i + PF);
     prev = fma(-__ldg(l + i), prev, x[i]);
     x[i] = prev;
   }
   double x2 = 0.0, x4 = 0.0;
   for (i -= 2; i >= 0; i -= 2) {  // u1, u2 hold u dinv: one FMA on the x2 dependency
+    if (i >= PF) {
+      prefetch_l1(dinv + i - PF);
+      prefetch_l1(u1 + i - PF);
+      prefetch_l1(u2 + i - PF);
+    }
     const double w = fma(-__ldg(u2 + i), x4, x[i] * __ldg(dinv + i));
     const double v = fma(-__ldg(u1 + i), x2, w);
     x[i] = v;
@@ -393,6 +405,11 @@ __device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n
   double z2 = 0.0, z4 = 0.0;       // zeta_{i-2}, zeta_{i-4}
   int i = p;
   for (; i < n; i += 2) {
+    if (i + PF < n) {
+      prefetch_l1(dinv + i + PF);
+      prefetch_l1(u1 + i + PF - 2);
+      prefetch_l1(u2 + i + PF - 4);
+    }
     double v = x[i];
     if (i >= 4) v = fma(-__ldg(u2 + i - 4), z4, v);
     if (i >= 2) v = fma(-__ldg(u1 + i - 2), z2, v);
@@ -402,6 +419,7 @@ __device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n
   }
   double xn = 0.0;
   for (i -= 2; i >= 0; i -= 2) {
+    if (i >= PF) prefetch_l1(l + i + 2 - PF);
     const double li = (i + 2 < n) ? __ldg(l + i + 2) : 0.0;
     xn = fma(-li, xn, x[i]);
     x[i] = xn;
