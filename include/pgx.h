@@ -97,7 +97,11 @@ enum pgx_opcode {
 enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_FWD_T = 3, PGX_DCT_BWD_T = 4 };
 
 /* Chain ops (DIFF, TDMA2, FDMA) act on the b consecutive slots a..a+b-1 at
- * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset. */
+ * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset.
+ * op.k of TDMA2 / FDMA / FDMA_T / POISSON / POISSON_T: PGX_CHAIN_WARP selects one
+ * warp per (line, parity) chain with a warp-parallel scan instead of one thread
+ * per chain (for passes with few lines). */
+#define PGX_CHAIN_WARP 1
 typedef struct pgx_op {
   int16_t code, a, b, arr, mat, len, par, k;
   double alpha;                    /* scalar; multiplied by par[par] when par >= 0 */

@@ -296,6 +296,24 @@ void pick_tile(pgx_program* P, int nlines, int maxlen, int nbuf, int fft_n) {
   if (nt < 64) nt = 64;
   if (nt > 512) nt = 512;
   P->nthreads = nt;
+  // Sequential chain sweeps with few lines in the launch (fewer chains than ~64 per SM)
+  // run one warp per (line, parity) chain with a warp-parallel scan.
+  bool chains = false;
+  for (int o = 0; o < P->nops; ++o) {
+    const int code = P->ops[o].code;
+    chains |= code == PGX_OP_TDMA2 || code == PGX_OP_FDMA || code == PGX_OP_FDMA_T || code == PGX_OP_POISSON ||
+              code == PGX_OP_POISSON_T;
+  }
+  if (chains && 2 * (int64_t)nlines < 152 * 64) {
+    for (int o = 0; o < P->nops; ++o) {
+      pgx_op& op = P->ops[o];
+      if (op.code == PGX_OP_TDMA2 || op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T ||
+          op.code == PGX_OP_POISSON || op.code == PGX_OP_POISSON_T)
+        op.k = (int16_t)(op.k | PGX_CHAIN_WARP);
+    }
+    int wt = 64 * tb;  // two chains (parities) per line, one warp each
+    P->nthreads = wt < 256 ? 256 : (wt > 1024 ? 1024 : wt);
+  }
 }
 
 pgx_op mk(int code, int a, int b = -1, int arr = -1, int mat = -1, int len = -1, int k = 0, double alpha = 1.0) {

@@ -242,6 +242,134 @@ __device__ __forceinline__ bool chain_of(const Ctx& c, int ns, int& s, int& t, i
 }
 __device__ __forceinline__ int nslot_of(const pgx_op& op) { return op.b > 1 ? op.b : 1; }
 
+// ------------------------------------------------- warp-parallel recurrences
+// With few lines (one large instance) a chain per thread leaves the GPU idle while
+// each chain walks n/2 dependent steps.  In the warp mode of a chain op
+// (op.k & PGX_CHAIN_WARP) one warp solves one (line, parity) chain: the lanes own
+// consecutive segments, each lane composes its segment's affine map, the maps are
+// scanned across the warp with shuffles, and every lane re-runs its segment from
+// its exact incoming state.  The work grows ~3x, the dependent path shrinks from
+// n/2 steps to ~n/32 + 5 combine levels.
+constexpr unsigned FULLMASK = 0xffffffffu;
+
+// y_q = b(q) + a(q) y_{q-1} for q = 0..m-1 (recurrence order), y_{-1} = 0; put(q, y).
+template <class FA, class FB, class FP>
+__device__ __forceinline__ void warp_rec1(int m, int lane, FA a, FB b, FP put) {
+  const int C = (m + 31) >> 5;
+  const int q0 = min(lane * C, m), q1 = min(q0 + C, m);
+  double A = 1.0, B = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    const double aq = a(q);
+    B = fma(aq, B, b(q));
+    A *= aq;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double Ap = __shfl_up_sync(FULLMASK, A, o), Bp = __shfl_up_sync(FULLMASK, B, o);
+    if (lane >= o) {
+      B = fma(A, Bp, B);
+      A *= Ap;
+    }
+  }
+  double y = __shfl_up_sync(FULLMASK, B, 1);
+  if (lane == 0) y = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    y = fma(a(q), y, b(q));
+    put(q, y);
+  }
+}
+
+// y_q = b(q) + a1(q) y_{q-1} + a2(q) y_{q-2}, y_{-1} = y_{-2} = 0; put(q, y).
+// Segment maps act on the state (y_q, y_{q-1}): s_out = M s_in + c.
+template <class FA1, class FA2, class FB, class FP>
+__device__ __forceinline__ void warp_rec2(int m, int lane, FA1 a1, FA2 a2, FB b, FP put) {
+  const int C = (m + 31) >> 5;
+  const int q0 = min(lane * C, m), q1 = min(q0 + C, m);
+  double m00 = 1.0, m01 = 0.0, m10 = 0.0, m11 = 1.0, c0 = 0.0, c1 = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    const double x1 = a1(q), x2 = a2(q);
+    const double n00 = fma(x2, m10, x1 * m00), n01 = fma(x2, m11, x1 * m01);
+    const double nc0 = fma(x2, c1, fma(x1, c0, b(q)));
+    m10 = m00;
+    m11 = m01;
+    c1 = c0;
+    m00 = n00;
+    m01 = n01;
+    c0 = nc0;
+  }
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double p00 = __shfl_up_sync(FULLMASK, m00, o), p01 = __shfl_up_sync(FULLMASK, m01, o);
+    const double p10 = __shfl_up_sync(FULLMASK, m10, o), p11 = __shfl_up_sync(FULLMASK, m11, o);
+    const double pc0 = __shfl_up_sync(FULLMASK, c0, o), pc1 = __shfl_up_sync(FULLMASK, c1, o);
+    if (lane >= o) {  // (M, c) after (P, pc): (M P, M pc + c)
+      const double r00 = fma(m01, p10, m00 * p00), r01 = fma(m01, p11, m00 * p01);
+      const double r10 = fma(m11, p10, m10 * p00), r11 = fma(m11, p11, m10 * p01);
+      const double s0 = fma(m01, pc1, fma(m00, pc0, c0)), s1 = fma(m11, pc1, fma(m10, pc0, c1));
+      m00 = r00;
+      m01 = r01;
+      m10 = r10;
+      m11 = r11;
+      c0 = s0;
+      c1 = s1;
+    }
+  }
+  double y1 = __shfl_up_sync(FULLMASK, c0, 1), y2 = __shfl_up_sync(FULLMASK, c1, 1);
+  if (lane == 0) y1 = y2 = 0.0;
+  for (int q = q0; q < q1; ++q) {
+    const double y = fma(a2(q), y2, fma(a1(q), y1, b(q)));
+    y2 = y1;
+    y1 = y;
+    put(q, y);
+  }
+}
+
+// The chain of parity p of an n-point line, x[p + 2k], k < m = (n - p + 1) / 2.
+__device__ __forceinline__ void fdma_chain_warp(double* x, const double* tab, int n, int p, int lane) {
+  const double* l = tab;
+  const double* dinv = tab + n;
+  const double* u1 = tab + 2 * n;
+  const double* u2 = tab + 3 * n;
+  const int m = (n - p + 1) >> 1;
+  // L: y_k = x_k - l_k y_{k-1}
+  warp_rec1(m, lane, [&](int q) { return -__ldg(l + p + 2 * q); }, [&](int q) { return x[p + 2 * q]; },
+            [&](int q, double y) { x[p + 2 * q] = y; });
+  __syncwarp();
+  // U (from the top): v_i = x_i dinv_i - (u1 dinv)_i v_{i+2} - (u2 dinv)_i v_{i+4}
+  warp_rec2(m, lane, [&](int q) { return -__ldg(u1 + p + 2 * (m - 1 - q)); },
+            [&](int q) { return -__ldg(u2 + p + 2 * (m - 1 - q)); },
+            [&](int q) { const int i = p + 2 * (m - 1 - q); return x[i] * __ldg(dinv + i); },
+            [&](int q, double y) { x[p + 2 * (m - 1 - q)] = y; });
+}
+
+__device__ __forceinline__ void fdma_t_chain_warp(double* x, const double* tab, int n, int p, int lane) {
+  const double* l = tab;
+  const double* dinv = tab + n;
+  const double* u1 = tab + 2 * n;
+  const double* u2 = tab + 3 * n;
+  const int m = (n - p + 1) >> 1;
+  // U^T on zeta = z / dinv: zeta_i = x_i - (u1 dinv)_{i-2} zeta_{i-2} - (u2 dinv)_{i-4} zeta_{i-4}; z = zeta dinv
+  warp_rec2(m, lane, [&](int q) { const int i = p + 2 * q; return i >= 2 ? -__ldg(u1 + i - 2) : 0.0; },
+            [&](int q) { const int i = p + 2 * q; return i >= 4 ? -__ldg(u2 + i - 4) : 0.0; },
+            [&](int q) { return x[p + 2 * q]; },
+            [&](int q, double y) { const int i = p + 2 * q; x[i] = y * __ldg(dinv + i); });
+  __syncwarp();
+  // L^T (from the top): x_i = z_i - l_{i+2} x_{i+2}
+  warp_rec1(m, lane, [&](int q) { const int i = p + 2 * (m - 1 - q); return i + 2 < n ? -__ldg(l + i + 2) : 0.0; },
+            [&](int q) { return x[p + 2 * (m - 1 - q)]; }, [&](int q, double y) { x[p + 2 * (m - 1 - q)] = y; });
+}
+
+__device__ __forceinline__ void tdma_chain_warp(double* x, const double* tab, int n, int p, int lane) {
+  const int m = (n - p + 1) >> 1;
+  // g_i = r_i x_i - (a r)_i g_{i-2};  x_i = g_i - w_i x_{i+2}
+  warp_rec1(m, lane, [&](int q) { return -__ldg(tab + 3 * (p + 2 * q)); },
+            [&](int q) { const int i = p + 2 * q; return x[i] * __ldg(tab + 3 * i + 1); },
+            [&](int q, double y) { x[p + 2 * q] = y; });
+  __syncwarp();
+  warp_rec1(m, lane, [&](int q) { return -__ldg(tab + 3 * (p + 2 * (m - 1 - q)) + 2); },
+            [&](int q) { return x[p + 2 * (m - 1 - q)]; }, [&](int q, double y) { x[p + 2 * (m - 1 - q)] = y; });
+}
+
 // (S^T S) x = d with the offset-2 TDMA; table interleaved per index i as
 // (aa_i, rden_i, w_i), so one long table serves every system length n:
 //   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}.
@@ -249,6 +377,19 @@ __device__ __forceinline__ int nslot_of(const pgx_op& op) { return op.b > 1 ? op
 __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   int s, t, p;
   const int ns = nslot_of(op);
+  if (op.k & PGX_CHAIN_WARP) {
+    const int lane = c.tid & 31, nw = c.nthreads >> 5;
+    for (int w = c.tid >> 5; w < 2 * c.tb * ns; w += nw) {
+      s = w / (2 * c.tb);
+      const int r = w - s * 2 * c.tb;
+      p = r / c.tb;
+      t = r - p * c.tb;
+      const int n = c.slen[op.a + s];
+      if (p >= n) continue;
+      tdma_chain_warp(slot_ptr(c, op.a + s) + t * c.lcap, I.mat[op.mat], n, p, lane);
+    }
+    return;
+  }
   for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
     Ctx cc = c;
     cc.tid = c.tid + base;
@@ -429,6 +570,24 @@ __device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n
 __device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line, bool transpose = false) {
   int s, t, p;
   const int ns = nslot_of(op);
+  if (op.k & PGX_CHAIN_WARP) {
+    const int lane = c.tid & 31, nw = c.nthreads >> 5;
+    for (int w = c.tid >> 5; w < 2 * c.tb * ns; w += nw) {
+      s = w / (2 * c.tb);
+      const int r = w - s * 2 * c.tb;
+      p = r / c.tb;
+      t = r - p * c.tb;
+      const int n = c.slen[op.a + s];
+      const int line = c.l0 + t;
+      if (p >= n || line >= c.nlines) continue;
+      const double* tab = I.mat[op.mat + (per_line ? 0 : s)];
+      if (per_line) tab += (size_t)line * 4 * n;
+      double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+      if (transpose) fdma_t_chain_warp(x, tab, n, p, lane);
+      else fdma_chain_warp(x, tab, n, p, lane);
+    }
+    return;
+  }
   for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
     Ctx cc = c;
     cc.tid = c.tid + base;

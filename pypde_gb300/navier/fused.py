@@ -664,7 +664,11 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
         elif o.code in (_lib.OP["DIFF"], _lib.OP["DIFF_T"]):
             width = max(width, max(o.b, 1))
     nt = max(256, 32 * -(-width * tb // 32))
-    return tb, min(nt, 1024)
+    # few chains in the whole launch: one warp per chain (scanned) instead of one thread
+    wc = chains and width * lines_total < 152 * 64
+    if wc:
+        nt = max(256, min(1024, 32 * width * tb))
+    return tb, min(nt, 1024), bool(wc)
 
 
 def _candidates(prog, lines_total, lcap, fft_n, max_lines):
@@ -683,6 +687,7 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
         tb = (SMEM_PER_SM // ctas - 2048) // per_line
         tbs.add(int(tb))
     tbs.update({1, 2, 4, 8, 16})
+    chains = any(o.code in _CHAIN_CODES for o in prog.ops)
     out = []
     for tb in sorted(tbs):
         tb = min(tb, 64, max(max_lines, 1))
@@ -694,8 +699,13 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
             continue
         for nt in (256, 512):
             nt = max(nt, 32 * -(-width * tb // 32))
-            if nt <= 1024 and (tb, nt) not in out:
-                out.append((tb, nt))
+            if nt <= 1024 and (tb, nt, False) not in out:
+                out.append((tb, nt, False))
+        if chains:  # warp-per-chain variants: a warp for each of the CTA's chains, up to 1024 threads
+            for nt in (256, min(1024, 32 * width * tb)):
+                nt = max(nt, 256)
+                if nt <= 1024 and (tb, nt, True) not in out:
+                    out.append((tb, nt, True))
     return out
 
 
@@ -757,7 +767,8 @@ class FusedBatch:
             I.fill(prog, insts[k])
         return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
 
-    def _group_launch(self, prog, d_insts, key, members, tb, nt):
+    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False):
+        """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode."""
         lcap, fft_n = key
         P = _lib.PgxProgram()
         P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
@@ -765,10 +776,12 @@ class FusedBatch:
         assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
         for i, o in enumerate(prog.ops):
             P.ops[i] = o
+            if wc and o.code in _CHAIN_CODES:
+                P.ops[i].k = o.k | _lib.CHAIN_WARP
         work = [(k, t) for k in members for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
         return {"name": prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
-                "key": key, "members": members, "prog": prog}
+                "key": key, "members": members, "prog": prog, "wc": bool(wc)}
 
     def _pass_launches(self, prog, tiles=None, index=None):
         d_insts = self._d_insts(prog)
@@ -778,9 +791,10 @@ class FusedBatch:
             tag = "%s#%d" % (prog.name, gi)
             if tiles and tag in tiles:
                 tb, nt = tiles[tag][:2]
+                wc = bool(tiles[tag][2]) if len(tiles[tag]) > 2 else False
             else:
-                tb, nt = _pick(prog, sum(lines), key[0], key[1], max(lines))
-            out.append(self._group_launch(prog, d_insts, key, members, tb, nt))
+                tb, nt, wc = _pick(prog, sum(lines), key[0], key[1], max(lines))
+            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, wc))
         return out
 
     def _build_launches(self, tiles=None):
@@ -790,7 +804,7 @@ class FusedBatch:
 
     @staticmethod
     def _tiles_of(launch_sets):
-        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads)
+        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads, L["wc"])
                 for group in launch_sets for gi, L in enumerate(group)}
 
     def tiles(self):
@@ -815,8 +829,8 @@ class FusedBatch:
                 prog, key, members = L0["prog"], L0["key"], L0["members"]
                 lines = [self.insts[k].lines(prog) for k in members]
                 best = None
-                for tb, nt in _candidates(prog, sum(lines), key[0], key[1], max(lines)):
-                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt)
+                for tb, nt, wc in _candidates(prog, sum(lines), key[0], key[1], max(lines)):
+                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc)
                     self._run_launch(L)
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -826,11 +840,11 @@ class FusedBatch:
                     torch.cuda.synchronize()
                     ms = a.elapsed_time(b) / reps
                     if verbose:
-                        print(prog.name, gi, tb, nt, round(ms, 4))
+                        print(prog.name, gi, tb, nt, wc, round(ms, 4))
                     if best is None or ms < best[0]:
-                        best = (ms, L, tb, nt)
+                        best = (ms, L, tb, nt, wc)
                 group[gi] = best[1]
-                chosen["%s#%d" % (prog.name, gi)] = (best[2], best[3], round(best[0], 4))
+                chosen["%s#%d" % (prog.name, gi)] = (best[2], best[3], best[4], round(best[0], 4))
         return chosen
 
     def autotune(self, reps=3, verbose=False):

@@ -128,3 +128,31 @@ def test_batched_heterogeneous(NS):
     for ns, (shape, ra, seed) in zip(solvers, specs):
         ref = oracle_run("linear", shape, dict(ra=ra, dt=0.005, dealias=True), seed, 1e-3, 3)
         compare(ns, ref, 1e-8)
+
+
+def test_warp_parallel_chains_match_sequential(NS):
+    """Every chain sweep in warp-per-chain (scanned) mode gives the one-thread-per-chain result
+    to rounding; the 65 x 33 and 129 x 65 instances exercise chains longer than a warp."""
+    from pypde_gb300.navier.fused import FusedBatch, _CHAIN_CODES
+    specs = [((65, 33), 1e5, 1), ((129, 65), 1e6, 2)]
+    outs = []
+    for warp in (False, True):
+        solvers = []
+        for shape, ra, seed in specs:
+            ns = NS(case="rbc", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers)
+        tiles = {}
+        for tag, (tb, nt, wc) in fb.tiles().items():
+            prog = fb.progs[[p.name for p in fb.progs].index(tag.split("#")[0])]
+            chains = any(o.code in _CHAIN_CODES for o in prog.ops)
+            tiles[tag] = (tb, max(nt, 256), warp and chains)
+        fb._build_launches(tiles)
+        assert any(L["wc"] for g in fb.launches for L in g) == warp
+        for _ in range(3):
+            fb.step_eager()
+        outs.append([ns.state() for ns in solvers])
+    for a, b in zip(*outs):
+        for k in a:
+            assert rel_err(b[k], a[k]) < 1e-12, k
