@@ -691,10 +691,8 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     out = []
     for tb in sorted(tbs):
         tb = min(tb, 64, max(max_lines, 1))
-        if fft_n > 1:
-            tb -= tb % 2
-            if tb < 2:
-                continue
+        if fft_n > 1 and tb > 1:  # FFT lines go in pairs; a single line (paired with zeros) gives
+            tb -= tb % 2          # twice the CTAs when an instance has few lines
         if tb < 1 or tb * per_line > SMEM_PER_SM - 2048:
             continue
         for nt in (256, 512):
