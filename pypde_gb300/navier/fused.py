@@ -38,7 +38,7 @@ from ..host import fdma_lu, pseudoinverse_d2, stencil_matrix, stencil_sub
 # fixed len[] indices
 L_LINES, L_N, L_M, L_NG, L_MG, L_ND, L_MD = range(7)
 # fixed par[] indices
-P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT = range(9)
+P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT, P_B, P_C = range(11)
 
 FFT_RADICES = (2, 3)
 
@@ -148,9 +148,17 @@ class Prog:
         self.add("TDMA2", s, b=count, mat="tdma_" + kind)
 
 
-def build_programs(tkind, fft):
+def build_programs(tkind, fft, rk3=False):
     """The eleven passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
-    ("CD" for the linear / zero cases, "CN" for rbc)."""
+    ("CD" for the linear / zero cases, "CN" for rbc).
+
+    ``rk3``: the passes of one stage of the three-stage IMEX Runge-Kutta step
+    (rbc2d_base.py:86-102).  The stage coefficients arrive as per-stage parameters
+    (dt a, 1/(dt a), b, c) and per-stage ADI tables; the convection of the stage,
+    b conv(u) + c conv(u_old) (rbc2d.py:252-378), is the product with the
+    combined velocity b u + c u_old, since conv is linear in the velocity.  P2
+    keeps the stage's physical velocities for the next stage (UXC, UZC) and reads
+    the previous stage's (UXO, UZO)."""
     P = []
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
@@ -178,6 +186,11 @@ def build_programs(tkind, fft):
         p.stencil(s, "CD")
         p.setlen(s, L_MD)
         p.dct(s, BWD, fft)
+    if rk3:
+        for s, C, O in ((0, "UXC", "UXO"), (1, "UZC", "UZO")):
+            p.store(s, C)
+            p.scale(s, par=P_B)
+            p.load_add(s, O, par=P_C)
     for F in "UVT":
         p.load(2, "A_" + F + "x", L_MG)
         p.stencil(2, "CD")
@@ -487,12 +500,14 @@ def host_tables(N, M, tk, dt, nu, kappa, scale, fd, adjoint=False):
     return t
 
 
-def instance_params(N, M, dealias, dt, nu, kappa, scale):
-    """len[] and par[] of one instance (indices L_* and P_*)."""
+def instance_params(N, M, dealias, dt, nu, kappa, scale, a=1.0, b=1.0, c=0.0):
+    """len[] and par[] of one instance (indices L_* and P_*) for the stage coefficients a, b, c
+    (IMEX Euler: 1, 1, 0)."""
     Nd, Md = (int(1.5 * N), int(1.5 * M)) if dealias else (N, M)
     sx, sz = scale
     lens = [0, N, M, N - 2, M - 2, Nd, Md]
-    par = [1.0 / sx, 1.0 / sz, -dt, dt, dt * kappa, -dt / sx, -dt / sz, -nu, 1.0 / dt]
+    da = dt * a
+    par = [1.0 / sx, 1.0 / sz, -dt, da, da * kappa, -da / sx, -da / sz, -nu, 1.0 / da, b, c]
     return lens, par
 
 
@@ -530,8 +545,9 @@ class _Instance:
                 "PRES": (N, M)}
 
     def __init__(self, ns, fft, views=None, bind=True):
-        if ns.nstage != 1 or ns.beta != 1.0:
-            raise NotImplementedError("the fused step covers IMEX Euler with beta = 1; use update() otherwise")
+        if ns.nstage not in (1, 3) or ns.beta != 1.0:
+            raise NotImplementedError("the fused step covers IMEX Euler and RK3 with beta = 1; use update() "
+                                      "otherwise")
         self.ns = ns
         N, M = ns.shape
         Nd, Md = (int(1.5 * N), int(1.5 * M)) if ns.dealias else (N, M)
@@ -562,6 +578,23 @@ class _Instance:
         host = host_tables(N, M, ns.T.xs[0].id, ns.dt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
         t.update({k: to_dev(v) for k, v in host.items()})
         self.tables = t
+        # per stage: parameters, ADI tables (lambda = dt a nu or dt a kappa) and the velocity arrays
+        # of the stage and of the previous one (RK3)
+        self.nstage = ns.nstage
+        self.stage_par, self.stage_tables, self.stage_arrays = [self.par], [{}], [{}]
+        if self.nstage == 3:
+            for k in ("UX_A", "UX_B", "UZ_A", "UZ_B"):
+                a[k] = z(Nd, Md)
+            self.stage_par, self.stage_tables, self.stage_arrays = [], [], []
+            for st in range(3):
+                ak, bk, ck = float(ns.a[st]), float(ns.b[st]), float(ns.c[st])
+                self.stage_par.append(instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale,
+                                                      ak, bk, ck)[1])
+                hs = host_tables(N, M, ns.T.xs[0].id, ns.dt * ak, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
+                self.stage_tables.append({k: to_dev(hs[k]) for k in ("Ax_U", "Ax_T", "Ay_U", "Ay_T")})
+                cur, old = ("A", "A") if st == 0 else (("B", "A") if st == 1 else ("A", "B"))
+                self.stage_arrays.append({"UXC": "UX_" + cur, "UZC": "UZ_" + cur, "UXO": "UX_" + old,
+                                          "UZO": "UZ_" + old})
         self.dct_x = _dct_tables(Nd, fft)
         self.dct_y = _dct_tables(Md, fft)
 
@@ -577,21 +610,23 @@ class _Instance:
     def lines(self, prog):
         return self.lens[prog.lines] if prog.lines else 0
 
-    def fill(self, prog, inst):
-        """Resolve ``prog``'s symbolic arrays / tables for this instance into a PgxInstance."""
+    def fill(self, prog, inst, stage=0):
+        """Resolve ``prog``'s symbolic arrays / tables for this instance (time-step stage ``stage``)
+        into a PgxInstance."""
+        amap, tmap = self.stage_arrays[stage], self.stage_tables[stage]
         for name, idx in prog.arrs.items():
-            t = self.arrays[name]
+            t = self.arrays[amap.get(name, name)]
             A = inst.arr[idx]
             A.ptr, A.s0, A.s1, A.n0, A.n1 = t.data_ptr(), t.stride(0), t.stride(1), t.shape[0], t.shape[1]
         dct = self.dct_x if prog.axis == 0 else self.dct_y
         for name, idx in prog.mats.items():
             base = name.split("#")[0]
-            v = dct[base] if base.startswith("dct") else self.tables[base]
+            v = dct[base] if base.startswith("dct") else tmap.get(base, self.tables.get(base))
             inst.mat[idx] = v if isinstance(v, int) else v.data_ptr()
         for i, n in enumerate(self.lens):
             inst.len[i] = n
         inst.len[L_LINES] = self.lens[prog.lines]
-        for i, v in enumerate(self.par):
+        for i, v in enumerate(self.stage_par[stage]):
             inst.par[i] = v
 
 
@@ -740,7 +775,11 @@ class FusedBatch:
                 views[key] = self.a_arena[aoff:aoff + r * c].view(r, c)
                 aoff += r * c
             self.insts.append(_Instance(ns, self.fft, views, bind))
-        self.progs = build_programs(tkinds.pop(), self.fft)
+        nst = {ns.nstage for ns in self.solvers}
+        if len(nst) != 1:
+            raise ValueError("all instances of a batch need the same integrator")
+        self.nstage = nst.pop()
+        self.progs = build_programs(tkinds.pop(), self.fft, rk3=self.nstage == 3)
         self._build_launches()
         self.graph = None
 
@@ -759,13 +798,13 @@ class FusedBatch:
             g.setdefault((lcap, fft_n), []).append(k)
         return sorted(g.items(), reverse=True)
 
-    def _d_insts(self, prog):
+    def _d_insts(self, prog, stage=0):
         insts = (_lib.PgxInstance * len(self.insts))()
         for k, I in enumerate(self.insts):
-            I.fill(prog, insts[k])
+            I.fill(prog, insts[k], stage)
         return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
 
-    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False):
+    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None):
         """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode."""
         lcap, fft_n = key
         P = _lib.PgxProgram()
@@ -778,27 +817,28 @@ class FusedBatch:
                 P.ops[i].k = o.k | _lib.CHAIN_WARP
         work = [(k, t) for k in members for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
-        return {"name": prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
+        return {"name": name or prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
                 "key": key, "members": members, "prog": prog, "wc": bool(wc)}
 
-    def _pass_launches(self, prog, tiles=None, index=None):
-        d_insts = self._d_insts(prog)
+    def _pass_launches(self, prog, tiles=None, stage=0):
+        d_insts = self._d_insts(prog, stage)
+        name = prog.name if stage == 0 else "%s@%d" % (prog.name, stage)
         out = []
         for gi, (key, members) in enumerate(self._groups(prog)):
             lines = [self.insts[k].lines(prog) for k in members]
-            tag = "%s#%d" % (prog.name, gi)
+            tag = "%s#%d" % (name, gi)
             if tiles and tag in tiles:
                 tb, nt = tiles[tag][:2]
                 wc = bool(tiles[tag][2]) if len(tiles[tag]) > 2 else False
             else:
                 tb, nt, wc = _pick(prog, sum(lines), key[0], key[1], max(lines))
-            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, wc))
+            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, wc, name))
         return out
 
     def _build_launches(self, tiles=None):
         """Launch descriptors of the forward passes; ``tiles`` = {"pass#group": (lines per CTA,
         threads)} overrides the default choice (e.g. another batch's autotuned tiles)."""
-        self.launches = [self._pass_launches(p, tiles) for p in self.progs]
+        self.launches = [self._pass_launches(p, tiles, st) for st in range(self.nstage) for p in self.progs]
 
     @staticmethod
     def _tiles_of(launch_sets):
@@ -828,7 +868,7 @@ class FusedBatch:
                 lines = [self.insts[k].lines(prog) for k in members]
                 best = None
                 for tb, nt, wc in _candidates(prog, sum(lines), key[0], key[1], max(lines)):
-                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc)
+                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"])
                     self._run_launch(L)
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -842,7 +882,7 @@ class FusedBatch:
                     if best is None or ms < best[0]:
                         best = (ms, L, tb, nt, wc)
                 group[gi] = best[1]
-                chosen["%s#%d" % (prog.name, gi)] = (best[2], best[3], best[4], round(best[0], 4))
+                chosen["%s#%d" % (L0["name"], gi)] = (best[2], best[3], best[4], round(best[0], 4))
         return chosen
 
     def autotune(self, reps=3, verbose=False):
@@ -898,6 +938,7 @@ class FusedBatch:
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""
         one = FusedBatch.__new__(FusedBatch)
         one.solvers, one.insts, one.fft, one.progs = [self.solvers[i]], [self.insts[i]], self.fft, self.progs
+        one.nstage = self.nstage
         one.state_arena = None
         one._build_launches()
         one.graph = None
@@ -909,7 +950,7 @@ class FusedBatch:
     def pass_work(self):
         """Algorithmic FP64 flops and HBM bytes per launch of every pass (all instances)."""
         out = []
-        for prog in self.progs:
+        for prog in self.progs * self.nstage:
             fl = by = 0.0
             for I in self.insts:
                 f, b = program_work(prog, I)

@@ -322,6 +322,8 @@ class FusedAdjoint(FusedBatch):
     """
 
     def __init__(self, solvers):
+        if any(ns.nstage != 1 for ns in solvers):
+            raise NotImplementedError("the reverse-mode fused step covers IMEX Euler")
         FusedBatch.__init__(self, solvers)
         self.bar_arena = torch.zeros_like(self.state_arena)
         off = 0

@@ -64,11 +64,12 @@ def test_host_matrices_match_oracle(N):
 @pytest.mark.parametrize("tkind", ["CD", "CN"])
 @pytest.mark.parametrize("fft", [True, False])
 def test_fused_programs_fit_the_abi(tkind, fft):
-    """Every fused pass respects the C-ABI limits and uses only slots it declares."""
+    """Every fused pass (Euler and RK3-stage variants) respects the C-ABI limits and uses only
+    slots it declares."""
     from pypde_gb300 import _lib
     from pypde_gb300.navier.fused import build_programs
-    progs = build_programs(tkind, fft)
-    assert len(progs) == 11
+    progs = build_programs(tkind, fft) + build_programs(tkind, fft, rk3=True)
+    assert len(progs) == 22
     uses_b = {_lib.OP[k] for k in ("AXPY", "MUL", "COPY")}
     for p in progs:
         assert len(p.ops) <= _lib.MAX_OPS, p.name

@@ -156,3 +156,42 @@ def test_warp_parallel_chains_match_sequential(NS):
     for a, b in zip(*outs):
         for k in a:
             assert rel_err(b[k], a[k]) < 1e-12, k
+
+
+RK3_CASES = [("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
+             ("rbc", (33, 17), dict(ra=1e5, dt=0.01, dealias=True)),
+             ("zero", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
+             ("linear", (40, 24), dict(ra=1e5, dt=0.01, dealias=True))]
+
+
+@pytest.mark.parametrize("case,shape,cfg", RK3_CASES, ids=[f"{c[0]}-{c[1][0]}x{c[1][1]}" for c in RK3_CASES])
+def test_fused_rk3_vs_oracle(NS, case, shape, cfg):
+    """Three-stage IMEX RK3 (rbc2d_base.py:86-102) as 3 x 11 fused passes against the oracle."""
+    from oracle import rbc2d as orb
+    ns = NS(case=case, shape=shape, pr=1.0, tsave=None, integrator="rk3", **cfg)
+    ns.set_temperature_noise(7, 1e-2)
+    f = ns.fused()
+    assert f.nstage == 3 and len(f.launches) == 33
+    f.step_eager()
+    ref = orb.NavierStokes(case=case, shape=shape, pr=1.0, tsave=None, integrator="rk3", **cfg)
+    orb.seeded_temperature(ref, 7, 1e-2)
+    ref.update()
+    compare(ns, ref, 1e-9)
+    for _ in range(4):
+        f.step_eager()
+        ref.update()
+    compare(ns, ref, 1e-8)
+
+
+def test_fused_rk3_golden(NS, golden):
+    """The reference's own RK3 run (33 x 33, Ra 1e5, dt 0.01, seed 3 noise 1e-2): 5 fused steps from a graph."""
+    ns = NS(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="rk3", tsave=None)
+    ns.set_temperature_noise(3, 1e-2)
+    assert rel_err(ns.state()["T"], golden["rbc_rk3_33_T0"]) < 1e-10
+    f = ns.fused()
+    f.capture(1)
+    for _ in range(5):
+        f.step()
+    st = ns.state()
+    for name in ("T", "U", "V", "P", "pres"):
+        assert rel_err(st[name], golden[f"rbc_rk3_33_s5_{name}"]) < 1e-8, name
