@@ -38,7 +38,7 @@ from ..host import fdma_lu, pseudoinverse_d2, stencil_matrix, stencil_sub
 # fixed len[] indices
 L_LINES, L_N, L_M, L_NG, L_MG, L_ND, L_MD = range(7)
 # fixed par[] indices
-P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT, P_B, P_C = range(11)
+P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT, P_B, P_C, P_TF = range(12)
 
 FFT_RADICES = (2, 3)
 
@@ -58,6 +58,9 @@ class Prog:
         self.name, self.axis, self.lines, self.nslots = name, axis, lines, nslots
         self.ops, self.arrs, self.mats = [], {}, {}
         self.has_dct = False
+        # variants: the same program run as several descriptors per instance, each renaming
+        # arrays / tables and overriding parameters ({"arrays": {}, "tables": {}, "par": {}})
+        self.variants = [{}]
 
     def _a(self, name):
         return self.arrs.setdefault(name, len(self.arrs))
@@ -507,7 +510,7 @@ def instance_params(N, M, dealias, dt, nu, kappa, scale, a=1.0, b=1.0, c=0.0):
     sx, sz = scale
     lens = [0, N, M, N - 2, M - 2, Nd, Md]
     da = dt * a
-    par = [1.0 / sx, 1.0 / sz, -dt, da, da * kappa, -da / sx, -da / sz, -nu, 1.0 / da, b, c]
+    par = [1.0 / sx, 1.0 / sz, -dt, da, da * kappa, -da / sx, -da / sz, -nu, 1.0 / da, b, c, 0.0]
     return lens, par
 
 
@@ -610,24 +613,28 @@ class _Instance:
     def lines(self, prog):
         return self.lens[prog.lines] if prog.lines else 0
 
-    def fill(self, prog, inst, stage=0):
-        """Resolve ``prog``'s symbolic arrays / tables for this instance (time-step stage ``stage``)
-        into a PgxInstance."""
+    def fill(self, prog, inst, stage=0, variant=None):
+        """Resolve ``prog``'s symbolic arrays / tables for this instance (time-step stage ``stage``,
+        program variant ``variant``) into a PgxInstance."""
+        variant = variant or {}
+        vmap, vtab, vpar = variant.get("arrays", {}), variant.get("tables", {}), variant.get("par", {})
         amap, tmap = self.stage_arrays[stage], self.stage_tables[stage]
         for name, idx in prog.arrs.items():
+            name = vmap.get(name, name)
             t = self.arrays[amap.get(name, name)]
             A = inst.arr[idx]
             A.ptr, A.s0, A.s1, A.n0, A.n1 = t.data_ptr(), t.stride(0), t.stride(1), t.shape[0], t.shape[1]
         dct = self.dct_x if prog.axis == 0 else self.dct_y
         for name, idx in prog.mats.items():
             base = name.split("#")[0]
+            base = vtab.get(base, base)
             v = dct[base] if base.startswith("dct") else tmap.get(base, self.tables.get(base))
             inst.mat[idx] = v if isinstance(v, int) else v.data_ptr()
         for i, n in enumerate(self.lens):
             inst.len[i] = n
         inst.len[L_LINES] = self.lens[prog.lines]
         for i, v in enumerate(self.stage_par[stage]):
-            inst.par[i] = v
+            inst.par[i] = vpar.get(i, v)
 
 
 def program_maxlen(prog, lens):
@@ -799,9 +806,13 @@ class FusedBatch:
         return sorted(g.items(), reverse=True)
 
     def _d_insts(self, prog, stage=0):
-        insts = (_lib.PgxInstance * len(self.insts))()
+        """Descriptors of every instance (x every program variant: instance k, variant v at
+        k * len(variants) + v)."""
+        nv = len(prog.variants)
+        insts = (_lib.PgxInstance * (len(self.insts) * nv))()
         for k, I in enumerate(self.insts):
-            I.fill(prog, insts[k], stage)
+            for v, var in enumerate(prog.variants):
+                I.fill(prog, insts[k * nv + v], stage, var)
         return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
 
     def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None):
@@ -815,7 +826,9 @@ class FusedBatch:
             P.ops[i] = o
             if wc and o.code in _CHAIN_CODES:
                 P.ops[i].k = o.k | _lib.CHAIN_WARP
-        work = [(k, t) for k in members for t in range(-(-self.insts[k].lines(prog) // tb))]
+        nv = len(prog.variants)
+        work = [(k * nv + v, t) for k in members for v in range(nv)
+                for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
         return {"name": name or prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
                 "key": key, "members": members, "prog": prog, "wc": bool(wc)}
@@ -831,7 +844,7 @@ class FusedBatch:
                 tb, nt = tiles[tag][:2]
                 wc = bool(tiles[tag][2]) if len(tiles[tag]) > 2 else False
             else:
-                tb, nt, wc = _pick(prog, sum(lines), key[0], key[1], max(lines))
+                tb, nt, wc = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
             out.append(self._group_launch(prog, d_insts, key, members, tb, nt, wc, name))
         return out
 
@@ -867,7 +880,7 @@ class FusedBatch:
                 prog, key, members = L0["prog"], L0["key"], L0["members"]
                 lines = [self.insts[k].lines(prog) for k in members]
                 best = None
-                for tb, nt, wc in _candidates(prog, sum(lines), key[0], key[1], max(lines)):
+                for tb, nt, wc in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines)):
                     L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"])
                     self._run_launch(L)
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -954,8 +967,8 @@ class FusedBatch:
             fl = by = 0.0
             for I in self.insts:
                 f, b = program_work(prog, I)
-                fl += f
-                by += b
+                fl += f * len(prog.variants)
+                by += b * len(prog.variants)
             out.append((prog.name, fl, by))
         return out
 

@@ -1,4 +1,4 @@
-"""Reverse-mode (discrete adjoint) fused step: thirteen line-program passes.
+"""Reverse-mode (discrete adjoint) fused step: fourteen line-program passes.
 
 The forward fused step (``fused.build_programs``) maps the state
 (U, V, T Galerkin coefficients and the Chebyshev pressure) to the next one.
@@ -14,7 +14,9 @@ sequence run backwards with every operator replaced by its transpose:
 
 The products ux * dF/dx and uz * dF/dz are linearised around the forward state
 of the step: pass R1 (the forward P1) recomputes A_F0 / A_Fx from that state,
-and Q2a / Q2b recompute ux, uz and the physical derivatives inside the pass.
+and Q2u / Q2f recompute ux, uz and the physical derivatives.  Q2f and Q1 are
+written once for a generic field F and run as three descriptors (U, V, T) of
+one launch, which triples the CTAs of a single instance.
 
   R1  x  forward P1 on the step's input state        -> A_F0, A_Fx
   Q10 y  velocity correction^T                       -> U*bar, V*bar, G1bar, G2bar
@@ -26,9 +28,10 @@ and Q2a / Q2b recompute ux, uz and the physical derivatives inside the pass.
   Q4  y  S_y^T, D_y^T, A_y^-T, B_y^T, (B S)_y^T      -> Q1bar, Q2bar
   Q3s x  A_x^-T, B_x^T, (B S)_x^T                    -> RHSbar, Ubar Vbar Tbar (old-time part)
   Q3  x  forward-DCT_x^T, pressure / buoyancy terms  -> Cbar, DPZbar, TSYbar, pres-bar
-  Q2a y  ux, uz; products^T for U, V; DCT_y^T chains -> A_F*bar, uxbar, uzbar (partial)
-  Q2b y  products^T for T; ux/uz chains; D_y^T, S_y^T -> A_F*bar, pres-bar, Tbar
-  Q1  x  DCT_x^T, D_x^T, S_x^T                       -> Ubar, Vbar, Tbar (convection part)
+  Q2u y  ux, uz (recomputed)                         -> UXP, UZP
+  Q2f y  per field: products^T, DCT_y^T chains       -> A_F*bar, uxbar / uzbar parts
+  Q2z y  ux/uz bar chains; D_y^T, S_y^T               -> A_U0bar, A_V0bar, pres-bar, Tbar
+  Q1  x  per field: DCT_x^T, D_x^T, S_x^T            -> Ubar, Vbar, Tbar (convection part)
 
 The gradient arrays are updated in place: they hold d/d(new state) on entry
 and d/d(old state) on exit, so a horizon is a loop of adjoint steps over the
@@ -39,13 +42,13 @@ import torch
 from .. import _lib
 from .._dev import DTYPE, device, to_dev
 from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX, P_MDTSZ,
-                    P_MNU, FusedBatch, Prog, _Instance, build_programs, host_tables)
+                    P_MNU, P_TF, FusedBatch, Prog, _Instance, build_programs, host_tables)
 
 BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
 
 def build_adjoint_programs(tkind, fft):
-    """R1 and the twelve transposed passes of one IMEX Euler step (beta = 1)."""
+    """R1 and the thirteen transposed passes of one IMEX Euler step (beta = 1)."""
     BWD, BWD_T, FWD_T = _lib.DCT_BWD, _lib.DCT_BWD_T, _lib.DCT_FWD_T
     kinds = {"U": "CD", "V": "CD", "T": tkind}
     ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
@@ -182,97 +185,91 @@ def build_adjoint_programs(tkind, fft):
         p.store(0, "bC_" + F)
     Q.append(p)
 
-    # Q2a / Q2b (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised
-    def velocities(p):
-        for s, F in ((0, "U"), (1, "V")):
-            p.load(s, "A_" + F + "0", L_MG)
-            p.stencil(s, "CD")
-            p.setlen(s, L_MD)
-            p.dct(s, BWD, fft)
-
-    def products_t(p, F, first):
-        p.load(4, "bC_" + F, L_M)
-        p.setlen(4, L_MD)
-        p.dct(4, FWD_T, fft)                      # conv bar
-        p.load(5, "A_" + F + "x", L_MG)
-        p.stencil(5, "CD")
-        p.setlen(5, L_MD)
-        p.dct(5, BWD, fft)                        # dF/dx (physical)
-        p.load(6, "A_" + F + "0", L_MG)
-        p.stencil(6, "CD")
-        p.diff(6)
-        p.scale(6, par=P_ISZ)
-        p.setlen(6, L_MD)
-        p.dct(6, BWD, fft)                        # dF/dz (physical)
-        p.mul(5, 4)
-        p.mul(6, 4)
-        if first:
-            p.copy(2, 5)
-            p.copy(3, 6)
-        else:
-            p.axpy(2, 5)
-            p.axpy(3, 6)
-        if F == "T":
-            p.load(6, "DTB1", L_MD)
-            p.mul(6, 4)
-            p.axpy(3, 6)
-        p.copy(5, 4)
-        p.mul(5, 0)                               # dF/dx bar = conv bar * ux
-        p.mul(4, 1)                               # dF/dz bar = conv bar * uz
-        p.dct(5, BWD_T, fft)
-        p.setlen(5, L_M)
-        p.stencil_t(5, "CD")
-        p.store(5, "bA_" + F + "x")
-        p.dct(4, BWD_T, fft)
-        p.setlen(4, L_M)
-        p.scale(4, par=P_ISZ)
-        p.diff_t(4)
-        p.stencil_t(4, "CD")
-        p.store(4, "bA_" + F + "0")
-
-    p = Prog("Q2a", 1, L_ND, 7)
-    velocities(p)
+    # Q2u / Q2f / Q2z (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised.
+    # Q2f runs once per field (three descriptors of one program, "variants"), so one instance
+    # gives three times the CTAs; the fields' contributions to ux bar, uz bar meet in Q2z.
+    p = Prog("Q2u", 1, L_ND, 2)
+    for s, F in ((0, "U"), (1, "V")):
+        p.load(s, "A_" + F + "0", L_MG)
+        p.stencil(s, "CD")
+        p.setlen(s, L_MD)
+        p.dct(s, BWD, fft)
     p.store(0, "UXP")
     p.store(1, "UZP")
-    products_t(p, "U", True)
-    products_t(p, "V", False)
-    p.store(2, "bUXP")
-    p.store(3, "bUZP")
     Q.append(p)
 
-    p = Prog("Q2b", 1, L_ND, 7)
+    p = Prog("Q2f", 1, L_ND, 5)
     p.load(0, "UXP", L_MD)
     p.load(1, "UZP", L_MD)
-    p.load(2, "bUXP", L_MD)
-    p.load(3, "bUZP", L_MD)
-    products_t(p, "T", False)
-    for s, F in ((2, "U"), (3, "V")):
+    p.load(2, "bC_F", L_M)
+    p.setlen(2, L_MD)
+    p.dct(2, FWD_T, fft)                          # conv bar
+    p.load(3, "A_Fx", L_MG)
+    p.stencil(3, "CD")
+    p.setlen(3, L_MD)
+    p.dct(3, BWD, fft)                            # dF/dx (physical)
+    p.load(4, "A_F0", L_MG)
+    p.stencil(4, "CD")
+    p.diff(4)
+    p.scale(4, par=P_ISZ)
+    p.setlen(4, L_MD)
+    p.dct(4, BWD, fft)                            # dF/dz (physical)
+    p.mul(3, 2)
+    p.store(3, "bUX_F")                           # ux bar, this field's part
+    p.load_add(4, "DTB1", par=P_TF)               # + DTB1 (temperature: the lift term)
+    p.mul(4, 2)
+    p.store(4, "bUZ_F")                           # uz bar, this field's part
+    p.copy(3, 2)
+    p.mul(3, 0)                                   # dF/dx bar = conv bar * ux
+    p.mul(2, 1)                                   # dF/dz bar = conv bar * uz
+    p.dct(3, BWD_T, fft)
+    p.setlen(3, L_M)
+    p.stencil_t(3, "CD")
+    p.store(3, "bA_Fx")
+    p.dct(2, BWD_T, fft)
+    p.setlen(2, L_M)
+    p.scale(2, par=P_ISZ)
+    p.diff_t(2)
+    p.stencil_t(2, "CD")
+    p.store(2, "bA_F0")
+    p.variants = [{"arrays": {"bC_F": "bC_" + F, "A_Fx": "A_" + F + "x", "A_F0": "A_" + F + "0",
+                              "bA_Fx": "bA_" + F + "x", "bA_F0": "bA_" + F + "0", "bUX_F": "bUX_" + F,
+                              "bUZ_F": "bUZ_" + F},
+                   "par": {P_TF: 1.0 if F == "T" else 0.0}} for F in "UVT"]
+    Q.append(p)
+
+    p = Prog("Q2z", 1, L_ND, 2)
+    for s, X, F in ((0, "bUX_", "U"), (1, "bUZ_", "V")):
+        p.load(s, X + "U", L_MD)
+        p.load_add(s, X + "V")
+        p.load_add(s, X + "T")
         p.dct(s, BWD_T, fft)
         p.setlen(s, L_M)
         p.stencil_t(s, "CD")
         p.store_add(s, "bA_" + F + "0")
-    p.load(4, "bDPZ", L_M)
-    p.diff_t(4)
-    p.store_add(4, "bPRES")
-    p.load(4, "bTSY", L_M)
-    p.stencil_t(4, "CD")
-    p.store_add(4, "bTG")
+    p.load(0, "bDPZ", L_M)
+    p.diff_t(0)
+    p.store_add(0, "bPRES")
+    p.load(0, "bTSY", L_M)
+    p.stencil_t(0, "CD")
+    p.store_add(0, "bTG")
     Q.append(p)
 
-    # Q1 (x, M-2 lines): A_F0 = Bwd_x S_x F; A_Fx = Bwd_x D_x S_x F / sx
+    # Q1 (x, M-2 lines), once per field: A_F0 = Bwd_x S_x F; A_Fx = Bwd_x D_x S_x F / sx
     p = Prog("Q1", 0, L_MG, 2)
-    for F in "UVT":
-        p.load(0, "bA_" + F + "0", L_ND)
-        p.dct(0, BWD_T, fft)
-        p.setlen(0, L_N)
-        p.load(1, "bA_" + F + "x", L_ND)
-        p.dct(1, BWD_T, fft)
-        p.setlen(1, L_N)
-        p.scale(1, par=P_ISX)
-        p.diff_t(1)
-        p.axpy(0, 1)
-        p.stencil_t(0, kinds[F])
-        p.store_add(0, "b" + F + "G")
+    p.load(0, "bA_F0", L_ND)
+    p.dct(0, BWD_T, fft)
+    p.setlen(0, L_N)
+    p.load(1, "bA_Fx", L_ND)
+    p.dct(1, BWD_T, fft)
+    p.setlen(1, L_N)
+    p.scale(1, par=P_ISX)
+    p.diff_t(1)
+    p.axpy(0, 1)
+    p.stencil_t(0, "F")
+    p.store_add(0, "bFG")
+    p.variants = [{"arrays": {"bA_F0": "bA_" + F + "0", "bA_Fx": "bA_" + F + "x", "bFG": "b" + F + "G"},
+                   "tables": {"sten_F": "sten_" + kinds[F]}} for F in "UVT"]
     Q.append(p)
     return Q
 
@@ -292,7 +289,7 @@ def adjoint_shapes(N, M, Nd, Md):
         sh["bA_" + F + "0"] = (Nd, M - 2)
         sh["bA_" + F + "x"] = (Nd, M - 2)
     sh["bDPZ"] = (N, M)
-    for k in ("UXP", "UZP", "bUXP", "bUZP"):
+    for k in ("UXP", "UZP", "bUX_U", "bUX_V", "bUX_T", "bUZ_U", "bUZ_V", "bUZ_T"):
         sh[k] = (Nd, Md)
     return sh
 

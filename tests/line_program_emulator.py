@@ -73,10 +73,19 @@ class Machine:
         self.arrays, self.tables, self.lens, self.par = arrays, tables, lens, par
 
     def run(self, prog):
+        """Run every variant of ``prog`` (one descriptor per variant on the device)."""
+        for var in prog.variants:
+            self._run(prog, var)
+
+    def _run(self, prog, var):
+        vmap, vtab, vpar = var.get("arrays", {}), var.get("tables", {}), var.get("par", {})
         L = self.lens[prog.lines]
         lcap = 8 + max(self.lens) * 2
-        arr_name = {i: k for k, i in prog.arrs.items()}
-        mat_name = {i: k.split("#")[0] for k, i in prog.mats.items()}
+        arr_name = {i: vmap.get(k, k) for k, i in prog.arrs.items()}
+        mat_name = {i: vtab.get(k.split("#")[0], k.split("#")[0]) for k, i in prog.mats.items()}
+        par = list(self.par)
+        for i, v in vpar.items():
+            par[i] = v
         axis = prog.axis
         nd = self.lens[5 + axis]
         dense = dense_dct_host(nd)
@@ -84,7 +93,7 @@ class Machine:
         slen = [0] * (prog.nslots + 1)
 
         def alpha(o):
-            return o.alpha * (self.par[o.par] if o.par >= 0 else 1.0)
+            return o.alpha * (par[o.par] if o.par >= 0 else 1.0)
 
         def view(name):
             A = self.arrays[name]

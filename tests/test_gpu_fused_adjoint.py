@@ -1,4 +1,4 @@
-"""The fused reverse-mode step (thirteen line-program passes) on the GPU.
+"""The fused reverse-mode step (fourteen line-program passes) on the GPU.
 
 One adjoint step is compared with the autograd vector-Jacobian product of the
 plain step (whose every operator runs a hand-written transposed kernel):
