@@ -194,7 +194,7 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ GPU side
-def build_batch(specs):
+def build_batch(specs, split=None):
     from pypde_gb300.navier.fused import FusedBatch
     from pypde_gb300.navier.rbc2d import NavierStokes
     solvers = []
@@ -203,7 +203,7 @@ def build_batch(specs):
                           integrator="eu", beta=1.0, tsave=None)
         ns.set_temperature_noise(seed, amp)
         solvers.append(ns)
-    return solvers, FusedBatch(solvers)
+    return solvers, FusedBatch(solvers, split=split)
 
 
 def time_steps(fn, steps, stream):
@@ -259,7 +259,7 @@ def run_gpu(args, rank, world):
                          "restatement of the reference path) in %d single-threaded processes, %.1f s of stepping"
                          % (len(sample), len(specs), steps_cpu, ncores, wall)}
 
-    solvers, fb = build_batch(specs)
+    solvers, fb = build_batch(specs, {"auto": None, "on": True, "off": False}[args.split])
     n_inst = len(solvers)
     stream = torch.cuda.current_stream()
     tuned = None
@@ -389,7 +389,9 @@ def run_gpu(args, rank, world):
         "dtype": "f64",
         "data": "synthetic: seeded U(-1,1) temperature noise on the conductive profile (seeds 100+i)",
         "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=n_inst), "instances_per_gpu": n_inst,
-                   "sizes": sorted({s[0] for s in specs}), "form": "batched, CUDA-graph replay of 10 fused passes",
+                   "sizes": sorted({s[0] for s in specs}),
+                   "form": "batched, CUDA-graph replay of %d fused passes%s" % (
+                       len(fb.progs), " (per-field convection passes)" if fb.split else ""),
                    "l2": "no flush: the working set (state %.1f MB + scratch %.1f MB) exceeds the 129 MB L2"
                          % (state_bytes / 1e6, work_bytes / 1e6), "parallelism": "instance-parallel"},
         "e2e": e2e,
@@ -611,6 +613,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
+    ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],
+                    help="per-field convection passes (auto: for batches of up to 4 instances)")
     ap.add_argument("--save-tiles", default=None)
     ap.add_argument("--adjoint-iters", type=int, default=50, help="descent iterations (-1: skip the adjoint part)")
     ap.add_argument("--adjoint-horizon", type=int, default=200)

@@ -151,39 +151,28 @@ class Prog:
         self.add("TDMA2", s, b=count, mat="tdma_" + kind)
 
 
-def build_programs(tkind, fft, rk3=False):
-    """The eleven passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
-    ("CD" for the linear / zero cases, "CN" for rbc).
-
-    ``rk3``: the passes of one stage of the three-stage IMEX Runge-Kutta step
-    (rbc2d_base.py:86-102).  The stage coefficients arrive as per-stage parameters
-    (dt a, 1/(dt a), b, c) and per-stage ADI tables; the convection of the stage,
-    b conv(u) + c conv(u_old) (rbc2d.py:252-378), is the product with the
-    combined velocity b u + c u_old, since conv is linear in the velocity.  P2
-    keeps the stage's physical velocities for the next stage (UXC, UZC) and reads
-    the previous stage's (UXO, UZO)."""
-    P = []
+def _split_convection_programs(tkind, fft, rk3):
+    """P1, P2u, P2, P3, P3r with P1 / P2 / P3 written once for a generic field F (variants)."""
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
-
-    # P1 (x, lines M-2): physical-in-x parts of F and dF/dx
+    P = []
     p = Prog("P1", 0, L_MG, 2)
-    for F in "UVT":
-        p.load(0, F + "G", L_NG)
-        p.stencil(0, kinds[F])
-        p.copy(1, 0)
-        p.diff(1)
-        p.scale(1, par=P_ISX)
-        p.setlen(0, L_ND)
-        p.dct(0, BWD, fft)
-        p.store(0, "A_" + F + "0")
-        p.setlen(1, L_ND)
-        p.dct(1, BWD, fft)
-        p.store(1, "A_" + F + "x")
+    p.load(0, "FG", L_NG)
+    p.stencil(0, "F")
+    p.copy(1, 0)
+    p.diff(1)
+    p.scale(1, par=P_ISX)
+    p.setlen(0, L_ND)
+    p.dct(0, BWD, fft)
+    p.store(0, "A_F0")
+    p.setlen(1, L_ND)
+    p.dct(1, BWD, fft)
+    p.store(1, "A_Fx")
+    p.variants = [{"arrays": {"FG": F + "G", "A_F0": "A_" + F + "0", "A_Fx": "A_" + F + "x"},
+                   "tables": {"sten_F": "sten_" + kinds[F]}} for F in "UVT"]
     P.append(p)
 
-    # P2 (y, lines Nd): velocities, products, forward y-transform; D_y pres; S_y T
-    p = Prog("P2", 1, L_ND, 4)
+    p = Prog("P2u", 1, L_ND, 2)
     for s, F in ((0, "U"), (1, "V")):
         p.load(s, "A_" + F + "0", L_MG)
         p.stencil(s, "CD")
@@ -194,56 +183,166 @@ def build_programs(tkind, fft, rk3=False):
             p.store(s, C)
             p.scale(s, par=P_B)
             p.load_add(s, O, par=P_C)
-    for F in "UVT":
-        p.load(2, "A_" + F + "x", L_MG)
-        p.stencil(2, "CD")
-        p.setlen(2, L_MD)
-        p.dct(2, BWD, fft)
-        p.mul(2, 0)
-        p.load(3, "A_" + F + "0", L_MG)
-        p.stencil(3, "CD")
-        p.diff(3)
-        p.scale(3, par=P_ISZ)
-        p.setlen(3, L_MD)
-        p.dct(3, BWD, fft)
-        p.mul(3, 1)
-        p.axpy(2, 3)
-        if F == "T":
-            p.load(3, "DTB1", L_MD)
-            p.mul(3, 1)
-            p.axpy(2, 3)
-        p.dct(2, FWD, fft)
-        p.setlen(2, L_M)
-        p.store(2, "C_" + F)
-    p.load(2, "PRES", L_M)
-    p.diff(2)
-    p.store(2, "DPZ")
-    p.load(2, "TG", L_MG)
-    p.stencil(2, "CD")
-    p.store(2, "TSY")
+    p.store(0, "UXP")
+    p.store(1, "UZP")
+    p.load(0, "PRES", L_M)
+    p.diff(0)
+    p.store(0, "DPZ")
+    p.load(0, "TG", L_MG)
+    p.stencil(0, "CD")
+    p.store(0, "TSY")
     P.append(p)
 
-    # P3 (x, lines M): forward x-transform and right-hand sides
-    p = Prog("P3", 0, L_M, 2)
-    for F in "UVT":
-        p.load(0, "C_" + F, L_ND)
-        p.dct(0, FWD, fft)
-        p.setlen(0, L_N)
-        p.scale(0, par=P_MDT)
-        if F == "U":
-            p.load(1, "PRES", L_N)
-            p.diff(1)
-            p.axpy(0, 1, par=P_MDTSX)
-        elif F == "V":
-            p.load_add(0, "DPZ", par=P_MDTSZ)
-            p.load_add(0, "TBCC", par=P_DT)
-            p.load(1, "TSY", L_NG)
-            p.stencil(1, tkind)
-            p.axpy(0, 1, par=P_DT)
-        else:
-            p.load_add(0, "DTB2", par=P_DTK)
-        p.store(0, "RHS_" + F)
+    p = Prog("P2", 1, L_ND, 4)
+    p.load(0, "UXP", L_MD)
+    p.load(1, "UZP", L_MD)
+    p.load(2, "A_Fx", L_MG)
+    p.stencil(2, "CD")
+    p.setlen(2, L_MD)
+    p.dct(2, BWD, fft)
+    p.mul(2, 0)
+    p.load(3, "A_F0", L_MG)
+    p.stencil(3, "CD")
+    p.diff(3)
+    p.scale(3, par=P_ISZ)
+    p.setlen(3, L_MD)
+    p.dct(3, BWD, fft)
+    p.load_add(3, "DTB1", par=P_TF)         # temperature: + the lift's dT/dz
+    p.mul(3, 1)
+    p.axpy(2, 3)
+    p.dct(2, FWD, fft)
+    p.setlen(2, L_M)
+    p.store(2, "C_F")
+    p.variants = [{"arrays": {"A_Fx": "A_" + F + "x", "A_F0": "A_" + F + "0", "C_F": "C_" + F},
+                   "par": {P_TF: 1.0 if F == "T" else 0.0}} for F in "UVT"]
     P.append(p)
+
+    p = Prog("P3", 0, L_M, 1)
+    p.load(0, "C_F", L_ND)
+    p.dct(0, FWD, fft)
+    p.setlen(0, L_N)
+    p.scale(0, par=P_MDT)
+    p.store(0, "RHS_F")
+    p.variants = [{"arrays": {"C_F": "C_" + F, "RHS_F": "RHS_" + F}} for F in "UVT"]
+    P.append(p)
+
+    p = Prog("P3r", 0, L_M, 2)
+    p.load(0, "PRES", L_N)
+    p.diff(0)
+    p.store_add(0, "RHS_U", par=P_MDTSX)
+    p.load(0, "DPZ", L_N, par=P_MDTSZ)
+    p.load_add(0, "TBCC", par=P_DT)
+    p.load(1, "TSY", L_NG)
+    p.stencil(1, tkind)
+    p.axpy(0, 1, par=P_DT)
+    p.store_add(0, "RHS_V")
+    p.load(0, "DTB2", L_N, par=P_DTK)
+    p.store_add(0, "RHS_T")
+    P.append(p)
+    return P
+
+
+def build_programs(tkind, fft, rk3=False, split=False):
+    """The eleven passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
+    ("CD" for the linear / zero cases, "CN" for rbc).
+
+    ``rk3``: the passes of one stage of the three-stage IMEX Runge-Kutta step
+    (rbc2d_base.py:86-102).  The stage coefficients arrive as per-stage parameters
+    (dt a, 1/(dt a), b, c) and per-stage ADI tables; the convection of the stage,
+    b conv(u) + c conv(u_old) (rbc2d.py:252-378), is the product with the
+    combined velocity b u + c u_old, since conv is linear in the velocity.  P2
+    keeps the stage's physical velocities for the next stage (UXC, UZC) and reads
+    the previous stage's (UXO, UZO).
+
+    ``split``: P1 - P3 as per-field programs run as three descriptors of one launch
+    (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3r (the non-convective
+    right-hand-side terms): the same transforms in twelve passes, with three times
+    the CTAs in the transform-heavy ones - for batches of few instances."""
+    P = []
+    BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
+    kinds = {"U": "CD", "V": "CD", "T": tkind}
+
+    if split:
+        P += _split_convection_programs(tkind, fft, rk3)
+    else:
+        # P1 (x, lines M-2): physical-in-x parts of F and dF/dx
+        p = Prog("P1", 0, L_MG, 2)
+        for F in "UVT":
+            p.load(0, F + "G", L_NG)
+            p.stencil(0, kinds[F])
+            p.copy(1, 0)
+            p.diff(1)
+            p.scale(1, par=P_ISX)
+            p.setlen(0, L_ND)
+            p.dct(0, BWD, fft)
+            p.store(0, "A_" + F + "0")
+            p.setlen(1, L_ND)
+            p.dct(1, BWD, fft)
+            p.store(1, "A_" + F + "x")
+        P.append(p)
+
+        # P2 (y, lines Nd): velocities, products, forward y-transform; D_y pres; S_y T
+        p = Prog("P2", 1, L_ND, 4)
+        for s, F in ((0, "U"), (1, "V")):
+            p.load(s, "A_" + F + "0", L_MG)
+            p.stencil(s, "CD")
+            p.setlen(s, L_MD)
+            p.dct(s, BWD, fft)
+        if rk3:
+            for s, C, O in ((0, "UXC", "UXO"), (1, "UZC", "UZO")):
+                p.store(s, C)
+                p.scale(s, par=P_B)
+                p.load_add(s, O, par=P_C)
+        for F in "UVT":
+            p.load(2, "A_" + F + "x", L_MG)
+            p.stencil(2, "CD")
+            p.setlen(2, L_MD)
+            p.dct(2, BWD, fft)
+            p.mul(2, 0)
+            p.load(3, "A_" + F + "0", L_MG)
+            p.stencil(3, "CD")
+            p.diff(3)
+            p.scale(3, par=P_ISZ)
+            p.setlen(3, L_MD)
+            p.dct(3, BWD, fft)
+            p.mul(3, 1)
+            p.axpy(2, 3)
+            if F == "T":
+                p.load(3, "DTB1", L_MD)
+                p.mul(3, 1)
+                p.axpy(2, 3)
+            p.dct(2, FWD, fft)
+            p.setlen(2, L_M)
+            p.store(2, "C_" + F)
+        p.load(2, "PRES", L_M)
+        p.diff(2)
+        p.store(2, "DPZ")
+        p.load(2, "TG", L_MG)
+        p.stencil(2, "CD")
+        p.store(2, "TSY")
+        P.append(p)
+
+        # P3 (x, lines M): forward x-transform and right-hand sides
+        p = Prog("P3", 0, L_M, 2)
+        for F in "UVT":
+            p.load(0, "C_" + F, L_ND)
+            p.dct(0, FWD, fft)
+            p.setlen(0, L_N)
+            p.scale(0, par=P_MDT)
+            if F == "U":
+                p.load(1, "PRES", L_N)
+                p.diff(1)
+                p.axpy(0, 1, par=P_MDTSX)
+            elif F == "V":
+                p.load_add(0, "DPZ", par=P_MDTSZ)
+                p.load_add(0, "TBCC", par=P_DT)
+                p.load(1, "TSY", L_NG)
+                p.stencil(1, tkind)
+                p.axpy(0, 1, par=P_DT)
+            else:
+                p.load_add(0, "DTB2", par=P_DTK)
+            p.store(0, "RHS_" + F)
+        P.append(p)
 
     # P3s (x, lines M): B_x, ADI x-sweep of the rhs and of the old-time terms B_x S_x F;
     # the six independent sweeps run as one multi-slot chain op
@@ -529,6 +628,8 @@ def scratch_shapes(N, M, Nd, Md):
         sh["Q2_" + F] = (N - 2, M - 2)
     sh["DPZ"] = (N, M)
     sh["TSY"] = (N - 2, M)
+    sh["UXP"] = (Nd, Md)
+    sh["UZP"] = (Nd, Md)
     for k in ("W1", "W2", "R1", "Y1", "Y2", "G1", "G2"):
         sh[k] = (N - 2, M)
     sh["R2"] = (N - 2, M - 2)
@@ -752,9 +853,13 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
 class FusedBatch:
     """Fused Euler step for a batch of NavierStokes instances (any sizes / Ra)."""
 
-    def __init__(self, solvers, bind=True):
+    SPLIT_MAX = 4
+
+    def __init__(self, solvers, bind=True, split=None):
         """``bind``: the solvers' fields become views of this batch's state arena (the default);
-        with bind=False the batch works on its own copy of the states."""
+        with bind=False the batch works on its own copy of the states.  ``split``: per-field
+        convection passes (more CTAs per instance; default for batches of up to SPLIT_MAX
+        instances)."""
         self.solvers = list(solvers)
         tkinds = {ns.T.xs[0].id for ns in self.solvers}
         if len(tkinds) != 1:
@@ -786,7 +891,9 @@ class FusedBatch:
         if len(nst) != 1:
             raise ValueError("all instances of a batch need the same integrator")
         self.nstage = nst.pop()
-        self.progs = build_programs(tkinds.pop(), self.fft, rk3=self.nstage == 3)
+        self.tkind = tkinds.pop()
+        self.split = len(self.solvers) <= self.SPLIT_MAX if split is None else bool(split)
+        self.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=self.split)
         self._build_launches()
         self.graph = None
 
@@ -950,8 +1057,9 @@ class FusedBatch:
     def single(self, i):
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""
         one = FusedBatch.__new__(FusedBatch)
-        one.solvers, one.insts, one.fft, one.progs = [self.solvers[i]], [self.insts[i]], self.fft, self.progs
-        one.nstage = self.nstage
+        one.solvers, one.insts, one.fft = [self.solvers[i]], [self.insts[i]], self.fft
+        one.nstage, one.tkind, one.split = self.nstage, self.tkind, True
+        one.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=True)
         one.state_arena = None
         one._build_launches()
         one.graph = None

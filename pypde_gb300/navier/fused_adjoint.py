@@ -47,14 +47,15 @@ from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_IDT, P_ISX, P_ISZ,
 BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
 
-def build_adjoint_programs(tkind, fft):
-    """R1 and the thirteen transposed passes of one IMEX Euler step (beta = 1)."""
+def build_adjoint_programs(tkind, fft, split=False):
+    """R1 and the thirteen transposed passes of one IMEX Euler step (beta = 1); R1 is the
+    forward P1 of the same form (``split``: per-field) as the batch's forward passes."""
     BWD, BWD_T, FWD_T = _lib.DCT_BWD, _lib.DCT_BWD_T, _lib.DCT_FWD_T
     kinds = {"U": "CD", "V": "CD", "T": tkind}
     ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
     Q = []
 
-    r1 = build_programs(tkind, fft)[0]
+    r1 = build_programs(tkind, fft, split=split)[0]
     r1.name = "R1"
     Q.append(r1)
 
@@ -289,7 +290,7 @@ def adjoint_shapes(N, M, Nd, Md):
         sh["bA_" + F + "0"] = (Nd, M - 2)
         sh["bA_" + F + "x"] = (Nd, M - 2)
     sh["bDPZ"] = (N, M)
-    for k in ("UXP", "UZP", "bUX_U", "bUX_V", "bUX_T", "bUZ_U", "bUZ_V", "bUZ_T"):
+    for k in ("bUX_U", "bUX_V", "bUX_T", "bUZ_U", "bUZ_V", "bUZ_T"):
         sh[k] = (Nd, Md)
     return sh
 
@@ -318,10 +319,10 @@ class FusedAdjoint(FusedBatch):
     taken from the current ``state_arena`` by the gradient w.r.t. that state.
     """
 
-    def __init__(self, solvers):
+    def __init__(self, solvers, split=None):
         if any(ns.nstage != 1 for ns in solvers):
             raise NotImplementedError("the reverse-mode fused step covers IMEX Euler")
-        FusedBatch.__init__(self, solvers)
+        FusedBatch.__init__(self, solvers, split=split)
         self.bar_arena = torch.zeros_like(self.state_arena)
         off = 0
         for I in self.insts:
@@ -332,7 +333,7 @@ class FusedAdjoint(FusedBatch):
                 off += r * c
             add_adjoint_buffers(I, views)
         tkind = self.solvers[0].T.xs[0].id
-        self.aprogs = build_adjoint_programs(tkind, self.fft)
+        self.aprogs = build_adjoint_programs(tkind, self.fft, self.split)
         self.alaunches = [self._pass_launches(p) for p in self.aprogs]
         self.agraph = None
 
@@ -430,7 +431,7 @@ class HorizonGradient:
                 v.fill_(1.0)
         self.rec = None
         if overlap:
-            self.rec = FusedBatch(fa.solvers, bind=False)
+            self.rec = FusedBatch(fa.solvers, bind=False, split=fa.split)
             self.rec._build_launches(fa.tiles())
             self.side = torch.cuda.Stream(device=dev)
         self.graphs = {}

@@ -114,3 +114,57 @@ def test_banded_tables_solve_and_transpose():
             else:
                 ref = np.linalg.solve(K.T if transpose else K, b)
             assert np.allclose(x, ref, rtol=0, atol=1e-10 * np.abs(ref).max()), (j, transpose)
+
+
+@pytest.mark.parametrize("N,M,tk,dealias", CASES, ids=["13x11-CD", "12x13-CN", "11x9-nodealias"])
+@pytest.mark.parametrize("rk3", [False, True], ids=["euler", "rk3-stage1"])
+def test_split_programs_give_the_same_step(N, M, tk, dealias, rk3):
+    """The per-field (variant) form of the convection passes computes the fused form's step."""
+    m, rng = make_machine(N, M, tk, dealias, 2)
+    if rk3:  # a middle RK3 stage: b, c and the previous stage's velocities all matter
+        m.par[9], m.par[10] = 5.0 / 12.0, -17.0 / 60.0
+        for k in ("UX_A", "UZ_A", "UX_B", "UZ_B"):
+            m.arrays[k] = rng.standard_normal(m.arrays["UXP"].shape)
+        for name, arr in (("UXC", "UX_B"), ("UZC", "UZ_B"), ("UXO", "UX_A"), ("UZO", "UZ_A")):
+            m.arrays[name] = m.arrays[arr]
+    X = {k: 1e-1 * rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    out = []
+    for split in (False, True):
+        for k in STATE:
+            m.arrays[k][...] = X[k]
+        for p in build_programs(tk, True, rk3=rk3, split=split):
+            m.run(p)
+        out.append({k: m.arrays[k].copy() for k in STATE})
+    for k in STATE:
+        scale = np.abs(out[0][k]).max()
+        assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * scale, k
+
+
+@pytest.mark.parametrize("tk", ["CD", "CN"])
+def test_adjoint_of_split_form_is_the_transpose(tk):
+    """R1 in per-field form: the adjoint passes remain the transpose of the (split) forward step."""
+    m, rng = make_machine(12, 13, tk, True, 3)
+    fwd, adj = build_programs(tk, True, split=True), build_adjoint_programs(tk, True, split=True)
+    X = {k: 1e-1 * rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    d = {k: rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    g = {k: rng.standard_normal(m.arrays[k].shape) for k in STATE}
+
+    def phi(Y):
+        for k in STATE:
+            m.arrays[k][...] = Y[k]
+        for p in fwd:
+            m.run(p)
+        return {k: m.arrays[k].copy() for k in STATE}
+
+    h = 1e-3
+    yp = phi({k: X[k] + h * d[k] for k in STATE})
+    ym = phi({k: X[k] - h * d[k] for k in STATE})
+    lhs = sum(float((g[k] * (yp[k] - ym[k])).sum()) / (2 * h) for k in STATE)
+    for k in STATE:
+        m.arrays[k][...] = X[k]
+        m.arrays["b" + k][...] = g[k]
+    m.arrays["bPG"][...] = 0.0
+    for p in adj:
+        m.run(p)
+    rhs = sum(float((m.arrays["b" + k] * d[k]).sum()) for k in STATE)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)
