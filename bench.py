@@ -159,7 +159,7 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -276,14 +276,16 @@ def run_gpu(args, rank, world):
     state_bytes = fb.state_arena.numel() * 8
     work_bytes = fb.scratch_bytes()
 
-    # warmup + timed region (graph replay), barrier + sync on both sides
+    # warmup + timed region (graph replay), barrier + sync on both sides; the clock sampler starts
+    # before the warm-up so that it is producing samples when the timed region begins
+    clocks = ClockSampler(local)
+    time.sleep(0.5)
     for _ in range(args.warmup):
         fb.step()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
     t0 = time.perf_counter()
     step_ms = time_steps(fb.step, args.steps, stream)
     wall = time.perf_counter() - t0
