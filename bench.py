@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "2D RBC FP64 steps/s at 1 GB300: plain vs batched-graph; adjoint grads/s at 1e-6 rel"
-FP64_PEAK_TFLOPS = 1.19  # measured DFMA throughput of this GB300 (profiles/gb300_fp64_probe.txt)
+FP64_PEAK_TFLOPS = 1.256  # measured DFMA throughput of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt)
 # DRAM bytes (read + write) of pass P2 on the 256-instance workload, one ncu capture of its three size-class
 # launches (profiles/line_program_batched_c4_launches.txt)
 P2_DRAM_BYTES = 154.5e6 + 37.6e6
@@ -337,8 +337,8 @@ def run_gpu(args, rank, world):
                 "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4),
                 "traffic": P2_DRAM_BYTES if (work[dom][0] == "P2" and args.workload == "c4" and n_inst == 256)
                 else None,
-                "peak_source": "measured DFMA peak of this GB300 (profiles/gb300_fp64_probe.txt); the "
-                               "driver-written peak file carries only HBM and bf16",
+                "peak_source": "measured DFMA peak of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt, "
+                               "pypde_gb300/csrc/fp64_probe.cu); the driver-written peak file carries only HBM and bf16",
                 "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2]}
     step_fl = sum(w[1] for w in work)
     step_fp64 = {"tflops": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12, 4),

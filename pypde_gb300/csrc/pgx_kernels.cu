@@ -7,7 +7,7 @@
 // operators, banded LU sweeps) runs on them, and results are stored back.
 //
 // All arithmetic is FP64.  On GB300 the FP64 pipe issues one warp instruction
-// per ~64 cycles per SM sub-partition (1.19 TFLOP/s for the whole GPU) and a
+// per ~64 cycles per SM sub-partition (1.26 TFLOP/s for the whole GPU) and a
 // dependent DFMA has ~67 cycles of latency, so the kernels count FP64
 // instructions, never divide in inner loops (reciprocals come from host-built
 // tables), and keep index arithmetic in integer registers.
