@@ -164,27 +164,46 @@ def build_adjoint_programs(tkind, fft, split=False):
     Q.append(p)
 
     # Q3 (x, M lines): RHS = -dt Fwd_x C (+ pressure gradient, buoyancy, lift terms)
-    p = Prog("Q3", 0, L_M, 2)
-    for F in "UVT":
-        p.load(0, "bRHS_" + F, L_N)
-        if F == "U":
-            p.copy(1, 0)
-            p.scale(1, par=P_MDTSX)
-            p.diff_t(1)
-            p.store_add(1, "bPRES")
-        elif F == "V":
-            p.copy(1, 0)
-            p.scale(1, par=P_MDTSZ)
-            p.store(1, "bDPZ")
-            p.copy(1, 0)
-            p.scale(1, par=P_DT)
-            p.stencil_t(1, tkind)
-            p.store(1, "bTSY")
-        p.scale(0, par=P_MDT)
+    if split:  # per field (Q3, three descriptors) and the other terms (Q3r)
+        p = Prog("Q3", 0, L_M, 1)
+        p.load(0, "bRHS_F", L_N, par=P_MDT)
         p.setlen(0, L_ND)
         p.dct(0, FWD_T, fft)
-        p.store(0, "bC_" + F)
-    Q.append(p)
+        p.store(0, "bC_F")
+        p.variants = [{"arrays": {"bRHS_F": "bRHS_" + F, "bC_F": "bC_" + F}} for F in "UVT"]
+        Q.append(p)
+        p = Prog("Q3r", 0, L_M, 1)
+        p.load(0, "bRHS_U", L_N, par=P_MDTSX)
+        p.diff_t(0)
+        p.store_add(0, "bPRES")
+        p.load(0, "bRHS_V", L_N, par=P_MDTSZ)
+        p.store(0, "bDPZ")
+        p.load(0, "bRHS_V", L_N, par=P_DT)
+        p.stencil_t(0, tkind)
+        p.store(0, "bTSY")
+        Q.append(p)
+    else:
+        p = Prog("Q3", 0, L_M, 2)
+        for F in "UVT":
+            p.load(0, "bRHS_" + F, L_N)
+            if F == "U":
+                p.copy(1, 0)
+                p.scale(1, par=P_MDTSX)
+                p.diff_t(1)
+                p.store_add(1, "bPRES")
+            elif F == "V":
+                p.copy(1, 0)
+                p.scale(1, par=P_MDTSZ)
+                p.store(1, "bDPZ")
+                p.copy(1, 0)
+                p.scale(1, par=P_DT)
+                p.stencil_t(1, tkind)
+                p.store(1, "bTSY")
+            p.scale(0, par=P_MDT)
+            p.setlen(0, L_ND)
+            p.dct(0, FWD_T, fft)
+            p.store(0, "bC_" + F)
+        Q.append(p)
 
     # Q2u / Q2f / Q2z (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised.
     # Q2f runs once per field (three descriptors of one program, "variants"), so one instance
