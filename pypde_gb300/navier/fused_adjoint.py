@@ -28,9 +28,9 @@ one launch, which triples the CTAs of a single instance.
   Q4  y  S_y^T, D_y^T, A_y^-T, B_y^T, (B S)_y^T      -> Q1bar, Q2bar
   Q3s x  A_x^-T, B_x^T, (B S)_x^T                    -> RHSbar, Ubar Vbar Tbar (old-time part)
   Q3  x  forward-DCT_x^T, pressure / buoyancy terms  -> Cbar, DPZbar, TSYbar, pres-bar
-  Q2u y  ux, uz (recomputed)                         -> UXP, UZP
+  Q2u y  ux, uz (recomputed); D_y^T, S_y^T          -> UXP, UZP, pres-bar, Tbar
   Q2f y  per field: products^T, DCT_y^T chains       -> A_F*bar, uxbar / uzbar parts
-  Q2z y  ux/uz bar chains; D_y^T, S_y^T               -> A_U0bar, A_V0bar, pres-bar, Tbar
+  Q2z y  per component: ux / uz bar chains           -> A_U0bar, A_V0bar
   Q1  x  per field: DCT_x^T, D_x^T, S_x^T            -> Ubar, Vbar, Tbar (convection part)
 
 The gradient arrays are updated in place: they hold d/d(new state) on entry
@@ -216,6 +216,12 @@ def build_adjoint_programs(tkind, fft, split=False):
         p.dct(s, BWD, fft)
     p.store(0, "UXP")
     p.store(1, "UZP")
+    p.load(0, "bDPZ", L_M)
+    p.diff_t(0)
+    p.store_add(0, "bPRES")
+    p.load(0, "bTSY", L_M)
+    p.stencil_t(0, "CD")
+    p.store_add(0, "bTG")
     Q.append(p)
 
     p = Prog("Q2f", 1, L_ND, 5)
@@ -258,21 +264,16 @@ def build_adjoint_programs(tkind, fft, split=False):
                    "par": {P_TF: 1.0 if F == "T" else 0.0}} for F in "UVT"]
     Q.append(p)
 
-    p = Prog("Q2z", 1, L_ND, 2)
-    for s, X, F in ((0, "bUX_", "U"), (1, "bUZ_", "V")):
-        p.load(s, X + "U", L_MD)
-        p.load_add(s, X + "V")
-        p.load_add(s, X + "T")
-        p.dct(s, BWD_T, fft)
-        p.setlen(s, L_M)
-        p.stencil_t(s, "CD")
-        p.store_add(s, "bA_" + F + "0")
-    p.load(0, "bDPZ", L_M)
-    p.diff_t(0)
-    p.store_add(0, "bPRES")
-    p.load(0, "bTSY", L_M)
+    p = Prog("Q2z", 1, L_ND, 1)   # per velocity component: ux bar -> A_U0 bar, uz bar -> A_V0 bar
+    p.load(0, "bX_U", L_MD)
+    p.load_add(0, "bX_V")
+    p.load_add(0, "bX_T")
+    p.dct(0, BWD_T, fft)
+    p.setlen(0, L_M)
     p.stencil_t(0, "CD")
-    p.store_add(0, "bTG")
+    p.store_add(0, "bA_X0")
+    p.variants = [{"arrays": {"bX_U": X + "U", "bX_V": X + "V", "bX_T": X + "T", "bA_X0": "bA_" + F + "0"}}
+                  for X, F in (("bUX_", "U"), ("bUZ_", "V"))]
     Q.append(p)
 
     # Q1 (x, M-2 lines), once per field: A_F0 = Bwd_x S_x F; A_Fx = Bwd_x D_x S_x F / sx
