@@ -157,3 +157,21 @@ def test_adjoint_step_vs_oracle_directional_derivative(torch):
     fa.adjoint_step()
     rhs = sum(float((bv[k].cpu().numpy() * di).sum()) for (k, _), di in zip(KEYS, d))
     assert abs(lhs - rhs) / abs(rhs) < 1e-8, (lhs, rhs)
+
+
+def test_horizon_gradient_forms_agree(torch):
+    """Sequential or two-stream reverse sweep, eager or one CUDA graph: the same gradient."""
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    ns = _ns("linear", (33, 17), ra=2e4)
+    X = _random_state(torch, ns, 4)[:3]
+    fa = FusedAdjoint([_ns("linear", (33, 17), ra=2e4)])
+    Xa = _arena_state(torch, fa, [X])
+    out = {}
+    for overlap in (False, True):
+        for graph in (False, True):
+            J, g = HorizonGradient(fa, 9, 4, overlap=overlap, graph=graph).value_and_grad(Xa)
+            out[(overlap, graph)] = (float(J[0]), g)
+    J0, g0 = out[(False, False)]
+    for key, (J, g) in out.items():
+        assert abs(J - J0) <= 1e-14 * J0, key
+        assert float((g - g0).abs().max() / g0.abs().max()) < 1e-13, key

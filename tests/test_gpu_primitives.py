@@ -177,6 +177,13 @@ def test_c_abi_rejects_bad_arguments(pg):
     assert L.pgx_dct1(1, 1, 1, 5, 1, 1, 1, 5, 5, 1, 2, 0, None) == 1  # axis 2
     assert L.pgx_fdma_solve(None, 1, 1, 1, 1, 0, None) == 4  # null plan
     assert L.pgx_cheb_diff(1, 1, 1, 1, 1, 1, 2, 1, 0, 1, None) == 1  # n < 3
+    # the transposed (reverse-mode) entry points check the same way
+    assert L.pgx_dct1(1, 1, 1, 5, 1, 1, 1, 5, 5, 1, 0, 5, None) == 1  # no mode 5
+    assert L.pgx_cheb_diff_t(1, 1, 1, 1, 1, 1, 2, 1, 0, 1, None) == 1  # n < 3
+    assert L.pgx_fdma_solve_t(None, 1, 1, 1, 1, 0, None) == 4  # null plan
+    assert L.pgx_poisson_solve_t(None, 1, 1, 1, 0, None) == 4
+    assert L.pgx_stencil_transpose(None, 1, 1, 1, 1, 1, 1, 1, 0, None) == 4
+    assert L.pgx_stencil_from_chebyshev_t(None, 1, 1, 1, 1, 1, 1, 1, 0, None) == 4
 
 
 RBC = [
