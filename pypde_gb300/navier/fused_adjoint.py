@@ -443,10 +443,14 @@ class HorizonGradient:
         # per step of a segment: the P1 outputs (physical-space operands of the convection terms),
         # which is all the reverse-mode passes read of the forward state
         self.traj = z(2 if overlap else 1, every, fa.a_arena.numel())
-        self.x0, self.x_in, self.g_out = z(n), z(n), z(n)
+        self.x0, self.x_in, self.g_out, self.y_out, self.g_in = z(n), z(n), z(n), z(n), z(n)
         self.J_out = z(len(fa.insts))
         self._mask = z(n)
         for d in fa.views(self._mask):
+            for v in d.values():
+                v.fill_(1.0)
+        self._state_mask = z(n)      # every input of a step: U, V, T, pres (not P)
+        for d in fa.views(self._state_mask, keys=("UG", "VG", "TG", "PRES")):
             for v in d.values():
                 v.fill_(1.0)
         self.rec = None
@@ -529,27 +533,42 @@ class HorizonGradient:
         join.record(self.side)
         main.wait_event(join)
 
-    def _run(self, grad):
-        self._forward_sweep(keep=grad)
+    def _run(self, what):
+        """'value': objective; 'grad': objective and gradient; 'map': Phi^H(x0) into y_out (keeping
+        the checkpoints); 'vjp': the reverse sweep of the last 'map' from the seed in g_in."""
+        if what in ("value", "grad", "map"):
+            self._forward_sweep(keep=what != "value")
+        if what == "map":
+            self.y_out.copy_(self.fa.state_arena)
+            return
+        if what == "vjp":
+            self.fa.bar_arena.copy_(self.g_in)
+            self._reverse_sweep()
+            self.g_out.copy_(self.fa.bar_arena * self._state_mask)
+            return
         J, seed = self._objective()
         self.J_out.copy_(J)
-        if grad:
+        if what == "grad":
             self.fa.bar_arena.copy_(seed)
             self._reverse_sweep()
             self.g_out.copy_((self.fa.bar_arena - seed) * self._mask)
 
-    def _replay(self, grad):
+    def _replay(self, what):
         if not self.use_graph:
-            self._run(grad)
+            self._run(what)
             return
-        g = self.graphs.get(grad)
+        g = self.graphs.get(what)
         if g is None:
-            self._run(grad)                 # warm-up outside the capture
+            saved = (self.ckpt.clone(), self.y_out.clone()) if what == "vjp" else None
+            self._run(what)                 # warm-up outside the capture
             torch.cuda.synchronize()
+            if saved is not None:           # the warm-up sweep must not disturb the checkpoints
+                self.ckpt.copy_(saved[0])
+                self.y_out.copy_(saved[1])
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
-                self._run(grad)
-            self.graphs[grad] = g
+                self._run(what)
+            self.graphs[what] = g
         g.replay()
 
     # ------------------------------------------------------------------- API
@@ -557,12 +576,48 @@ class HorizonGradient:
         """J per instance for the initial states X (arena-shaped; only U, V, T entries are used)."""
         self.x_in.copy_(X)
         self.x0.copy_(self.x_in * self._mask)
-        self._replay(False)
+        self._replay("value")
         return self.J_out.clone()
 
     def value_and_grad(self, X):
         """(J per instance, dJ/dX arena-shaped: U, V, T entries; zero elsewhere)."""
         self.x_in.copy_(X)
         self.x0.copy_(self.x_in * self._mask)
-        self._replay(True)
+        self._replay("grad")
         return self.J_out.clone(), self.g_out.clone()
+
+    # -- the horizon map and its vector-Jacobian product (for FusedHorizon)
+    def forward_map(self, X):
+        """Phi^H(X) over the whole state (U, V, T, P, pres in the arena layout); keeps the checkpoints
+        for ``vjp``."""
+        self.x0.copy_(X)
+        self._replay("map")
+        return self.y_out.clone()
+
+    def vjp(self, gY):
+        """d<gY, Phi^H(X)>/dX for the X of the last ``forward_map`` (P is not an input of a step:
+        its entries of the result are zero, and a gradient on the final P is not propagated)."""
+        self.g_in.copy_(gY)
+        self._replay("vjp")
+        return self.g_out.clone()
+
+
+
+class FusedHorizon(torch.autograd.Function):
+    """Y = Phi^H(X) on the fused passes, differentiable: backward runs the fused reverse-mode
+    passes over the checkpointed horizon.  X and Y are whole-batch state arenas (``fa.views``
+    gives the per-instance U, V, T, P, pres); the gradient flows to U, V, T and pres.
+
+        hg = HorizonGradient(FusedAdjoint(solvers), nsteps=200, every=20)
+        Y = FusedHorizon.apply(X, hg)       # X.requires_grad_()
+        loss = any_function_of(Y, X); loss.backward()
+    """
+
+    @staticmethod
+    def forward(ctx, X, hg):
+        ctx.hg = hg
+        return hg.forward_map(X.detach())
+
+    @staticmethod
+    def backward(ctx, gY):
+        return ctx.hg.vjp(gY.contiguous()), None

@@ -175,3 +175,30 @@ def test_horizon_gradient_forms_agree(torch):
     for key, (J, g) in out.items():
         assert abs(J - J0) <= 1e-14 * J0, key
         assert float((g - g0).abs().max() / g0.abs().max()) < 1e-13, key
+
+
+def test_fused_horizon_autograd_function(torch):
+    """FusedHorizon (torch.autograd.Function over the fused passes): a loss written in torch on the
+    horizon's output back-propagates through the fused reverse sweep; equals HorizonGradient and the
+    autograd gradient of the plain step."""
+    from pypde_gb300.navier.adjoint import ResidualObjective
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, FusedHorizon, HorizonGradient
+    H, every = 10, 4
+    ns = _ns("linear", (33, 33))
+    X = _random_state(torch, ns, 6)[:3]
+    J_ref, g_ref = ResidualObjective(ns, H, every).value_and_grad(X)
+    fa = FusedAdjoint([_ns("linear", (33, 33))])
+    hg = HorizonGradient(fa, H, every)
+    Xa = _arena_state(torch, fa, [X]).requires_grad_(True)
+    mask = torch.zeros_like(Xa)
+    for v in fa.views(mask)[0].values():
+        v.fill_(1.0)
+    Y = FusedHorizon.apply(Xa, hg)
+    J = torch.sqrt((((Y - Xa) * mask) ** 2).sum())
+    J.backward()
+    assert abs(float(J) - J_ref) / J_ref < 1e-10
+    gv = fa.views(Xa.grad)[0]
+    for k, r in zip(("TG", "UG", "VG"), g_ref):
+        assert rel_err(gv[k].cpu().numpy(), r.cpu().numpy()) < 1e-9, k
+    J2, g2 = hg.value_and_grad(Xa.detach())
+    assert float((g2 - Xa.grad).abs().max() / g2.abs().max()) < 1e-12
