@@ -73,7 +73,7 @@ static int check_program(const pgx_program* P) {
     if (uses_b && (op.b < 0 || op.b >= P->nslots)) return PGX_E_ARG;
     const bool chain = op.code == PGX_OP_DIFF || op.code == PGX_OP_DIFF_T || op.code == PGX_OP_TDMA2 ||
                        op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T;
-    if (chain && op.a + (op.b > 1 ? op.b : 1) > P->nslots) return PGX_E_ARG;
+    if ((chain || op.code == PGX_OP_DCT) && op.a + (op.b > 1 ? op.b : 1) > P->nslots) return PGX_E_ARG;
     if (chain && (op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T) && op.mat + (op.b > 1 ? op.b : 1) > PGX_MAX_MAT)
       return PGX_E_ARG;
     if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;

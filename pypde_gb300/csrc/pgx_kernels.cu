@@ -30,6 +30,15 @@ __host__ __device__ inline int pgx_fft_stride(int n) {
   return ((n - 1) & 1) == 0 ? (n - 1) : 2 * (n - 1);
 }
 
+// Slots transformed together by one DCT op (op.b), the most of any DCT op of the program:
+// the FFT buffers hold that many slots' line pairs.
+__host__ __device__ inline int pgx_fft_slots(const pgx_program& P) {
+  int fs = 1;
+  for (int o = 0; o < P.nops; ++o)
+    if (P.ops[o].code == PGX_OP_DCT && P.ops[o].b > fs) fs = P.ops[o].b;
+  return fs;
+}
+
 namespace pgx {
 
 // 2k for k < PGX_LMAX: multipliers of the derivative recurrence, read through
@@ -813,15 +822,20 @@ __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double
 // The backward pre-scale (-1)^j w_j is common to x_j and x_{N-j} (N even) and
 // applied to u_j, d_j; the forward post-scale to the outputs.
 __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  // op.b > 1: the transforms of slots a .. a+b-1 (same length and mode) go through every
+  // phase together: one barrier per phase for all of them, b times the parallel work.
+  const int ns = nslot_of(op);
   const int n = c.slen[op.a];
   const int N = n - 1, H = N / 2;
   const DctScale ds = dct_scale(op.k, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
-  double* x = slot_ptr(c, op.a);
   const int npairs = (c.tb + 1) >> 1;
+  const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
   // fold
-  for (int idx = c.tid; idx < npairs * N; idx += c.nthreads) {
-    const int pr = idx / N, j = idx - pr * N;
+  for (int idx = c.tid; idx < nall * N; idx += c.nthreads) {
+    const int P = idx / N, j = idx - P * N;
+    const int sl = P / npairs, pr = P - sl * npairs;
+    const double* x = slot_ptr(c, op.a + sl);
     const int t0 = 2 * pr;
     const bool two = t0 + 1 < c.tb;
     const double sn = -__ldg(&tw[j].y);
@@ -837,13 +851,14 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       ua *= sg;
       ub *= sg;
     }
-    c.f0[pr * c.fft_stride + j] = make_double2(ua, ub);
+    c.f0[P * c.fft_stride + j] = make_double2(ua, ub);
   }
-  // y_1: one warp per line
+  // y_1: one warp per line (line lt = sl * tb + t)
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
-    for (int t = warp; t < c.tb; t += nw) {
-      const double* xl = x + t * c.lcap;
+    for (int lt = warp; lt < ns * c.tb; lt += nw) {
+      const int sl = lt / c.tb, t = lt - sl * c.tb;
+      const double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
       double acc = 0.0;
       for (int j = 1 + lane; j < H; j += 32) {
         double d = xl[j] - xl[N - j];
@@ -853,16 +868,16 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       const double d0 = (xl[0] - xl[N]) * (ds.has_pre ? ds.pre(0, N) : 1.0);
-      if (lane == 0) c.ybuf[t] = fma(2.0, acc, d0);
+      if (lane == 0) c.ybuf[lt] = fma(2.0, acc, d0);
     }
   }
   __syncthreads();
-  // FFT of length N over the pairs
+  // FFT of length N over all pairs
   double2* bufs[2] = {c.f0, c.f1};
   int cur = 0, Ns = 1;
   for (int rem = N; rem > 1;) {
     const int R = next_radix(rem);
-    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, npairs, x, ds, 2);
+    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, nall, nullptr, ds, 2);
     cur ^= 1;
     Ns *= R;
     rem /= R;
@@ -870,12 +885,14 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
   const double2* Z = bufs[cur];
   // untangle: even outputs, odd increments
-  for (int idx = c.tid; idx < npairs * (H + 1); idx += c.nthreads) {
-    const int pr = idx / (H + 1), m = idx - pr * (H + 1);
+  for (int idx = c.tid; idx < nall * (H + 1); idx += c.nthreads) {
+    const int P = idx / (H + 1), m = idx - P * (H + 1);
+    const int sl = P / npairs, pr = P - sl * npairs;
+    double* x = slot_ptr(c, op.a + sl);
     const int t0 = 2 * pr;
     const bool two = t0 + 1 < c.tb;
-    const double2 zm = Z[pr * c.fft_stride + m];
-    const double2 zn = Z[pr * c.fft_stride + (m == 0 ? 0 : N - m)];
+    const double2 zm = Z[P * c.fft_stride + m];
+    const double2 zn = Z[P * c.fft_stride + (m == 0 ? 0 : N - m)];
     double ya = zm.x + zn.x, yb = zm.y + zn.y;
     if (ds.has_post) {
       const double sc = ds.post(2 * m, N);
@@ -888,8 +905,8 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       x[t0 * c.lcap + 2 * m + 1] = zn.y - zm.y;
       if (two) x[(t0 + 1) * c.lcap + 2 * m + 1] = zm.x - zn.x;
     } else if (m == 0) {
-      x[t0 * c.lcap + 1] = c.ybuf[t0];
-      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[t0 + 1];
+      x[t0 * c.lcap + 1] = c.ybuf[sl * c.tb + t0];
+      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
     }
   }
   __syncthreads();
@@ -898,8 +915,9 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
     const int chunk = (H + 31) / 32;
     const double osc = ds.has_post ? ds.post(1, N) : 1.0;  // the same for every odd k < N
-    for (int t = warp; t < c.tb; t += nw) {
-      double* xl = x + t * c.lcap;
+    for (int lt = warp; lt < ns * c.tb; lt += nw) {
+      const int sl = lt / c.tb, t = lt - sl * c.tb;
+      double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
       const int m0 = lane * chunk, m1 = min(m0 + chunk, H);
       double run = 0.0;
       for (int m = m0; m < m1; ++m) run += xl[2 * m + 1];
@@ -920,20 +938,31 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 
 // DCT-I of the slot (length n) in place: the folded half-length algorithm for
 // even n - 1, otherwise paired lines through a length-2(n-1) FFT (stockham_stage).
+__device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_instance& I);
+
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
   if (((n - 1) & 1) == 0 && n >= 3) {
     op_dct_even(c, op, I);
     return;
   }
+  const int ns = nslot_of(op);  // paired-line path: one slot after the other
+  for (int sl = 0; sl < ns; ++sl) {
+    dct_paired_slot(c, op.a + sl, op, I);
+    __syncthreads();
+  }
+}
+
+__device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_instance& I) {
+  const int n = c.slen[slot];
   if (2 * (n - 1) > c.fft_stride) {  // buffer sized for a shorter even length: refuse loudly
-    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a, idx, n);
+    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, slot, idx, n);
     return;
   }
   const int N = n - 1, L = 2 * N;
   const DctScale ds = dct_scale(op.k, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
-  double* x = slot_ptr(c, op.a);
+  double* x = slot_ptr(c, slot);
   const int npairs = (c.tb + 1) >> 1;
   int nst = 0;
   for (int rem = L; rem > 1; rem /= next_radix(rem)) ++nst;
@@ -990,9 +1019,10 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   c.sm = BATCHED ? smem_dyn + (sizeof(pgx_instance) + 7) / 8 : smem_dyn;
   size_t off = (size_t)nbuf * c.tb * c.lcap;
   c.fft_stride = pgx_fft_stride(P.fft_n);
+  const int fs = pgx_fft_slots(P);
   c.f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
-  c.f1 = c.f0 + (size_t)((c.tb + 1) >> 1) * c.fft_stride;
-  c.ybuf = reinterpret_cast<double*>(c.f1 + (size_t)((c.tb + 1) >> 1) * c.fft_stride);
+  c.f1 = c.f0 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride;
+  c.ybuf = reinterpret_cast<double*>(c.f1 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride);
   for (int s = 0; s < nbuf; ++s) c.phys[s] = s;
   for (int s = 0; s < PGX_MAX_SLOTS; ++s) c.slen[s] = 0;
   c.spare = P.nslots;
@@ -1035,11 +1065,12 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   }
 }
 
-__global__ void line_program_single(const __grid_constant__ pgx_program P, const __grid_constant__ pgx_instance I) {
+// Up to 1024 threads a block (one warp per chain line): at most 64 registers a thread.
+__global__ void __launch_bounds__(1024) line_program_single(const __grid_constant__ pgx_program P, const __grid_constant__ pgx_instance I) {
   run_program<false>(P, I, blockIdx.x);
 }
 
-__global__ void line_program_batched(const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts,
+__global__ void __launch_bounds__(1024) line_program_batched(const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts,
                                      const int32_t* __restrict__ work) {
   extern __shared__ __align__(16) double smem_dyn[];
   pgx_instance* sI = reinterpret_cast<pgx_instance*>(smem_dyn);
@@ -1060,7 +1091,8 @@ extern "C" int64_t pgx_program_smem(const pgx_program* P) {
   int64_t nbuf = P->nslots + 1;
   int64_t doubles = nbuf * P->tb * P->lcap;
   doubles += doubles & 1;
-  if (P->fft_n > 1) doubles += 2 * 2 * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + P->tb + 1;
+  const int64_t fs = pgx_fft_slots(*P);
+  if (P->fft_n > 1) doubles += 2 * 2 * fs * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + fs * P->tb + 1;
   return doubles * 8;
 }
 

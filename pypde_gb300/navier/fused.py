@@ -112,12 +112,16 @@ class Prog:
     _DENSE_DCT = {_lib.DCT_FWD: "dct_fwd", _lib.DCT_BWD: "dct_bwd", _lib.DCT_FWD_T: "dct_fwd_t",
                   _lib.DCT_BWD_T: "dct_bwd_t"}
 
-    def dct(self, s, mode, fft):
+    def dct(self, s, mode, fft, count=1):
+        """DCT-I (``mode``) of slots s .. s+count-1, which hold lines of one length: one DCT
+        op for all of them (each phase of the transform runs over every slot's lines at once),
+        or ``count`` dense-matrix ops."""
         self.has_dct = True
         if fft:
-            self.add("DCT", s, mat="dct", k=mode)
+            self.add("DCT", s, b=count, mat="dct", k=mode)
         else:
-            self.add("DENSE", s, mat=self._DENSE_DCT[mode], len=L_ND + self.axis)
+            for i in range(count):
+                self.add("DENSE", s + i, mat=self._DENSE_DCT[mode], len=L_ND + self.axis)
 
     def banded(self, s, name, off0, ndiag, rows):
         self.add("BANDED", s, b=off0, mat=name, len=rows, k=ndiag)
@@ -163,10 +167,9 @@ def _split_convection_programs(tkind, fft, rk3):
     p.diff(1)
     p.scale(1, par=P_ISX)
     p.setlen(0, L_ND)
-    p.dct(0, BWD, fft)
-    p.store(0, "A_F0")
     p.setlen(1, L_ND)
-    p.dct(1, BWD, fft)
+    p.dct(0, BWD, fft, count=2)
+    p.store(0, "A_F0")
     p.store(1, "A_Fx")
     p.variants = [{"arrays": {"FG": F + "G", "A_F0": "A_" + F + "0", "A_Fx": "A_" + F + "x"},
                    "tables": {"sten_F": "sten_" + kinds[F]}} for F in "UVT"]
@@ -177,7 +180,7 @@ def _split_convection_programs(tkind, fft, rk3):
         p.load(s, "A_" + F + "0", L_MG)
         p.stencil(s, "CD")
         p.setlen(s, L_MD)
-        p.dct(s, BWD, fft)
+    p.dct(0, BWD, fft, count=2)
     if rk3:
         for s, C, O in ((0, "UXC", "UXO"), (1, "UZC", "UZO")):
             p.store(s, C)
@@ -199,14 +202,13 @@ def _split_convection_programs(tkind, fft, rk3):
     p.load(2, "A_Fx", L_MG)
     p.stencil(2, "CD")
     p.setlen(2, L_MD)
-    p.dct(2, BWD, fft)
-    p.mul(2, 0)
     p.load(3, "A_F0", L_MG)
     p.stencil(3, "CD")
     p.diff(3)
     p.scale(3, par=P_ISZ)
     p.setlen(3, L_MD)
-    p.dct(3, BWD, fft)
+    p.dct(2, BWD, fft, count=2)
+    p.mul(2, 0)
     p.load_add(3, "DTB1", par=P_TF)         # temperature: + the lift's dT/dz
     p.mul(3, 1)
     p.axpy(2, 3)
@@ -274,10 +276,9 @@ def build_programs(tkind, fft, rk3=False, split=False):
             p.diff(1)
             p.scale(1, par=P_ISX)
             p.setlen(0, L_ND)
-            p.dct(0, BWD, fft)
-            p.store(0, "A_" + F + "0")
             p.setlen(1, L_ND)
-            p.dct(1, BWD, fft)
+            p.dct(0, BWD, fft, count=2)
+            p.store(0, "A_" + F + "0")
             p.store(1, "A_" + F + "x")
         P.append(p)
 
@@ -287,7 +288,7 @@ def build_programs(tkind, fft, rk3=False, split=False):
             p.load(s, "A_" + F + "0", L_MG)
             p.stencil(s, "CD")
             p.setlen(s, L_MD)
-            p.dct(s, BWD, fft)
+        p.dct(0, BWD, fft, count=2)
         if rk3:
             for s, C, O in ((0, "UXC", "UXO"), (1, "UZC", "UZO")):
                 p.store(s, C)
@@ -297,14 +298,13 @@ def build_programs(tkind, fft, rk3=False, split=False):
             p.load(2, "A_" + F + "x", L_MG)
             p.stencil(2, "CD")
             p.setlen(2, L_MD)
-            p.dct(2, BWD, fft)
-            p.mul(2, 0)
             p.load(3, "A_" + F + "0", L_MG)
             p.stencil(3, "CD")
             p.diff(3)
             p.scale(3, par=P_ISZ)
             p.setlen(3, L_MD)
-            p.dct(3, BWD, fft)
+            p.dct(2, BWD, fft, count=2)
+            p.mul(2, 0)
             p.mul(3, 1)
             p.axpy(2, 3)
             if F == "T":
@@ -323,25 +323,26 @@ def build_programs(tkind, fft, rk3=False, split=False):
         P.append(p)
 
         # P3 (x, lines M): forward x-transform and right-hand sides
-        p = Prog("P3", 0, L_M, 2)
-        for F in "UVT":
-            p.load(0, "C_" + F, L_ND)
-            p.dct(0, FWD, fft)
-            p.setlen(0, L_N)
-            p.scale(0, par=P_MDT)
+        p = Prog("P3", 0, L_M, 4)
+        for i, F in enumerate("UVT"):
+            p.load(i, "C_" + F, L_ND)
+        p.dct(0, FWD, fft, count=3)
+        for i, F in enumerate("UVT"):
+            p.setlen(i, L_N)
+            p.scale(i, par=P_MDT)
             if F == "U":
-                p.load(1, "PRES", L_N)
-                p.diff(1)
-                p.axpy(0, 1, par=P_MDTSX)
+                p.load(3, "PRES", L_N)
+                p.diff(3)
+                p.axpy(i, 3, par=P_MDTSX)
             elif F == "V":
-                p.load_add(0, "DPZ", par=P_MDTSZ)
-                p.load_add(0, "TBCC", par=P_DT)
-                p.load(1, "TSY", L_NG)
-                p.stencil(1, tkind)
-                p.axpy(0, 1, par=P_DT)
+                p.load_add(i, "DPZ", par=P_MDTSZ)
+                p.load_add(i, "TBCC", par=P_DT)
+                p.load(3, "TSY", L_NG)
+                p.stencil(3, tkind)
+                p.axpy(i, 3, par=P_DT)
             else:
-                p.load_add(0, "DTB2", par=P_DTK)
-            p.store(0, "RHS_" + F)
+                p.load_add(i, "DTB2", par=P_DTK)
+            p.store(i, "RHS_" + F)
         P.append(p)
 
     # P3s (x, lines M): B_x, ADI x-sweep of the rhs and of the old-time terms B_x S_x F;
@@ -772,6 +773,19 @@ def fft_bytes_per_line(fft_n):
 SMEM_PER_SM = 227 * 1024
 
 
+def _fft_slots(prog, sd=False):
+    """Slots of the widest DCT op: the FFT buffers hold that many slots' lines (one with
+    ``sd``, the DCT ops split into one op per slot)."""
+    if sd:
+        return 1
+    return max([max(o.b, 1) for o in prog.ops if o.code == _lib.OP["DCT"]] or [1])
+
+
+# A multi-slot DCT op saves barriers, but its FFT buffers take shared memory from the
+# tile: past this transform length each slot's lines alone fill the CTA's threads.
+JOINT_DCT_MAX_N = 257
+
+
 def _pick(prog, lines_total, lcap, fft_n, max_lines):
     """Lines per CTA and threads for one pass over ``lines_total`` lines (all instances).
 
@@ -782,7 +796,8 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     warp of chains.
     """
     nbuf = prog.nslots + 1
-    per_line = 8 * nbuf * lcap + fft_bytes_per_line(fft_n)
+    sd = _fft_slots(prog) > 1 and fft_n > JOINT_DCT_MAX_N
+    per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
     chains = any(o.code in [_lib.OP[k] for k in CHAIN_OPS] for o in prog.ops)
     if fft_n > 1:
         budget = SMEM_PER_SM // 2 - 2048
@@ -811,14 +826,22 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     wc = chains and width * lines_total < 152 * 64
     if wc:
         nt = max(256, min(1024, 32 * width * tb))
-    return tb, min(nt, 1024), bool(wc)
+    return tb, min(nt, 1024), bool(wc), sd
 
 
 def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     """Tile shapes the autotuner tries for one pass: lines per CTA chosen so that 1, 2, 3
-    or 4 CTAs fit an SM's shared memory, plus small tiles for short passes."""
+    or 4 CTAs fit an SM's shared memory, plus small tiles for short passes; programs with
+    multi-slot DCT ops also with the DCTs one slot at a time (smaller FFT buffers)."""
+    out = []
+    for sd in ((False, True) if _fft_slots(prog) > 1 and fft_n > 1 else (False,)):
+        out += _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd)
+    return out
+
+
+def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd):
     nbuf = prog.nslots + 1
-    per_line = 8 * nbuf * lcap + fft_bytes_per_line(fft_n)
+    per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
     width = 1
     for o in prog.ops:
         if o.code in _CHAIN_CODES:
@@ -840,13 +863,13 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
             continue
         for nt in (256, 512):
             nt = max(nt, 32 * -(-width * tb // 32))
-            if nt <= 1024 and (tb, nt, False) not in out:
-                out.append((tb, nt, False))
+            if nt <= 1024 and (tb, nt, False, sd) not in out:
+                out.append((tb, nt, False, sd))
         if chains:  # warp-per-chain variants: a warp for each of the CTA's chains, up to 1024 threads
             for nt in (256, min(1024, 32 * width * tb)):
                 nt = max(nt, 256)
-                if nt <= 1024 and (tb, nt, True) not in out:
-                    out.append((tb, nt, True))
+                if nt <= 1024 and (tb, nt, True, sd) not in out:
+                    out.append((tb, nt, True, sd))
     return out
 
 
@@ -922,14 +945,21 @@ class FusedBatch:
                 I.fill(prog, insts[k * nv + v], stage, var)
         return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
 
-    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None):
-        """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode."""
+    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None, sd=False):
+        """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode;
+        ``sd``: multi-slot DCT ops as one op per slot."""
         lcap, fft_n = key
+        ops = []
+        for o in prog.ops:
+            if sd and o.code == _lib.OP["DCT"] and o.b > 1:
+                ops += [_lib.op("DCT", a=o.a + i, b=1, mat=o.mat, k=o.k) for i in range(o.b)]
+            else:
+                ops.append(o)
         P = _lib.PgxProgram()
         P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
-        P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(prog.ops), fft_n, nt
-        assert len(prog.ops) <= _lib.MAX_OPS, (prog.name, len(prog.ops))
-        for i, o in enumerate(prog.ops):
+        P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), fft_n, nt
+        assert len(ops) <= _lib.MAX_OPS, (prog.name, len(ops))
+        for i, o in enumerate(ops):
             P.ops[i] = o
             if wc and o.code in _CHAIN_CODES:
                 P.ops[i].k = o.k | _lib.CHAIN_WARP
@@ -938,7 +968,7 @@ class FusedBatch:
                 for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
         return {"name": name or prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
-                "key": key, "members": members, "prog": prog, "wc": bool(wc)}
+                "key": key, "members": members, "prog": prog, "wc": bool(wc), "sd": bool(sd)}
 
     def _pass_launches(self, prog, tiles=None, stage=0):
         d_insts = self._d_insts(prog, stage)
@@ -948,11 +978,10 @@ class FusedBatch:
             lines = [self.insts[k].lines(prog) for k in members]
             tag = "%s#%d" % (name, gi)
             if tiles and tag in tiles:
-                tb, nt = tiles[tag][:2]
-                wc = bool(tiles[tag][2]) if len(tiles[tag]) > 2 else False
+                tb, nt, wc, sd = (tuple(tiles[tag][:4]) + (False, False))[:4]
             else:
-                tb, nt, wc = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
-            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, wc, name))
+                tb, nt, wc, sd = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
+            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, bool(wc), name, bool(sd)))
         return out
 
     def _build_launches(self, tiles=None):
@@ -962,7 +991,7 @@ class FusedBatch:
 
     @staticmethod
     def _tiles_of(launch_sets):
-        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads, L["wc"])
+        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads, L["wc"], L["sd"])
                 for group in launch_sets for gi, L in enumerate(group)}
 
     def tiles(self):
@@ -987,8 +1016,8 @@ class FusedBatch:
                 prog, key, members = L0["prog"], L0["key"], L0["members"]
                 lines = [self.insts[k].lines(prog) for k in members]
                 best = None
-                for tb, nt, wc in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines)):
-                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"])
+                for tb, nt, wc, sd in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines)):
+                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"], sd)
                     self._run_launch(L)
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -998,11 +1027,11 @@ class FusedBatch:
                     torch.cuda.synchronize()
                     ms = a.elapsed_time(b) / reps
                     if verbose:
-                        print(prog.name, gi, tb, nt, wc, round(ms, 4))
+                        print(prog.name, gi, tb, nt, wc, sd, round(ms, 4))
                     if best is None or ms < best[0]:
-                        best = (ms, L, tb, nt, wc)
+                        best = (ms, L, tb, nt, wc, sd)
                 group[gi] = best[1]
-                chosen["%s#%d" % (L0["name"], gi)] = (best[2], best[3], best[4], round(best[0], 4))
+                chosen["%s#%d" % (L0["name"], gi)] = (best[2], best[3], best[4], best[5], round(best[0], 4))
         return chosen
 
     def autotune(self, reps=3, verbose=False):

@@ -183,26 +183,27 @@ def build_adjoint_programs(tkind, fft, split=False):
         p.store(0, "bTSY")
         Q.append(p)
     else:
-        p = Prog("Q3", 0, L_M, 2)
-        for F in "UVT":
-            p.load(0, "bRHS_" + F, L_N)
+        p = Prog("Q3", 0, L_M, 4)
+        for i, F in enumerate("UVT"):
+            p.load(i, "bRHS_" + F, L_N)
             if F == "U":
-                p.copy(1, 0)
-                p.scale(1, par=P_MDTSX)
-                p.diff_t(1)
-                p.store_add(1, "bPRES")
+                p.copy(3, i)
+                p.scale(3, par=P_MDTSX)
+                p.diff_t(3)
+                p.store_add(3, "bPRES")
             elif F == "V":
-                p.copy(1, 0)
-                p.scale(1, par=P_MDTSZ)
-                p.store(1, "bDPZ")
-                p.copy(1, 0)
-                p.scale(1, par=P_DT)
-                p.stencil_t(1, tkind)
-                p.store(1, "bTSY")
-            p.scale(0, par=P_MDT)
-            p.setlen(0, L_ND)
-            p.dct(0, FWD_T, fft)
-            p.store(0, "bC_" + F)
+                p.copy(3, i)
+                p.scale(3, par=P_MDTSZ)
+                p.store(3, "bDPZ")
+                p.copy(3, i)
+                p.scale(3, par=P_DT)
+                p.stencil_t(3, tkind)
+                p.store(3, "bTSY")
+            p.scale(i, par=P_MDT)
+            p.setlen(i, L_ND)
+        p.dct(0, FWD_T, fft, count=3)
+        for i, F in enumerate("UVT"):
+            p.store(i, "bC_" + F)
         Q.append(p)
 
     # Q2u / Q2f / Q2z (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised.
@@ -213,7 +214,7 @@ def build_adjoint_programs(tkind, fft, split=False):
         p.load(s, "A_" + F + "0", L_MG)
         p.stencil(s, "CD")
         p.setlen(s, L_MD)
-        p.dct(s, BWD, fft)
+    p.dct(0, BWD, fft, count=2)
     p.store(0, "UXP")
     p.store(1, "UZP")
     p.load(0, "bDPZ", L_M)
@@ -233,13 +234,12 @@ def build_adjoint_programs(tkind, fft, split=False):
     p.load(3, "A_Fx", L_MG)
     p.stencil(3, "CD")
     p.setlen(3, L_MD)
-    p.dct(3, BWD, fft)                            # dF/dx (physical)
     p.load(4, "A_F0", L_MG)
     p.stencil(4, "CD")
     p.diff(4)
     p.scale(4, par=P_ISZ)
     p.setlen(4, L_MD)
-    p.dct(4, BWD, fft)                            # dF/dz (physical)
+    p.dct(3, BWD, fft, count=2)                   # dF/dx, dF/dz (physical)
     p.mul(3, 2)
     p.store(3, "bUX_F")                           # ux bar, this field's part
     p.load_add(4, "DTB1", par=P_TF)               # + DTB1 (temperature: the lift term)
@@ -248,11 +248,10 @@ def build_adjoint_programs(tkind, fft, split=False):
     p.copy(3, 2)
     p.mul(3, 0)                                   # dF/dx bar = conv bar * ux
     p.mul(2, 1)                                   # dF/dz bar = conv bar * uz
-    p.dct(3, BWD_T, fft)
+    p.dct(2, BWD_T, fft, count=2)
     p.setlen(3, L_M)
     p.stencil_t(3, "CD")
     p.store(3, "bA_Fx")
-    p.dct(2, BWD_T, fft)
     p.setlen(2, L_M)
     p.scale(2, par=P_ISZ)
     p.diff_t(2)
@@ -279,10 +278,9 @@ def build_adjoint_programs(tkind, fft, split=False):
     # Q1 (x, M-2 lines), once per field: A_F0 = Bwd_x S_x F; A_Fx = Bwd_x D_x S_x F / sx
     p = Prog("Q1", 0, L_MG, 2)
     p.load(0, "bA_F0", L_ND)
-    p.dct(0, BWD_T, fft)
-    p.setlen(0, L_N)
     p.load(1, "bA_Fx", L_ND)
-    p.dct(1, BWD_T, fft)
+    p.dct(0, BWD_T, fft, count=2)
+    p.setlen(0, L_N)
     p.setlen(1, L_N)
     p.scale(1, par=P_ISX)
     p.diff_t(1)

@@ -173,7 +173,9 @@ class Machine:
             elif op == "DCT":
                 n = slen[a]
                 C = dense_dct_host(n)[DCT_NAME[o.k]]
-                slot[a, :, :n] = slot[a, :, :n] @ C.T
+                for s in range(max(o.b, 1)):    # one length for all slots of the op
+                    assert slen[a + s] == n, (prog.name, a + s, slen[a + s], n)
+                    slot[a + s, :, :n] = slot[a + s, :, :n] @ C.T
             elif op == "DENSE":
                 name = mat_name[o.mat]
                 A = dense[name] if name.startswith("dct") else self.tables[name]

@@ -144,7 +144,7 @@ def test_warp_parallel_chains_match_sequential(NS):
             solvers.append(ns)
         fb = FusedBatch(solvers)
         tiles = {}
-        for tag, (tb, nt, wc) in fb.tiles().items():
+        for tag, (tb, nt, wc, sd) in fb.tiles().items():
             prog = fb.progs[[p.name for p in fb.progs].index(tag.split("#")[0])]
             chains = any(o.code in _CHAIN_CODES for o in prog.ops)
             tiles[tag] = (tb, max(nt, 256), warp and chains)
@@ -156,6 +156,33 @@ def test_warp_parallel_chains_match_sequential(NS):
     for a, b in zip(*outs):
         for k in a:
             assert rel_err(b[k], a[k]) < 1e-12, k
+
+
+def test_joint_and_serial_dct_ops_agree(NS):
+    """Multi-slot DCT ops (all slots' lines through each transform phase together) give the
+    result of one DCT op per slot exactly; 97-point lines take the folded even path, 28-point
+    lines the paired-line path."""
+    from pypde_gb300.navier.fused import FusedBatch, _fft_slots
+    specs = [((65, 33), 1e5, 1), ((19, 33), 1e4, 2)]
+    outs = []
+    for sd in (False, True):
+        solvers = []
+        for shape, ra, seed in specs:
+            ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers)
+        assert fb.fft
+        tiles = {tag: (tb, nt, wc, sd) for tag, (tb, nt, wc, _) in fb.tiles().items()}
+        fb._build_launches(tiles)
+        joint = [L for g in fb.launches for L in g if _fft_slots(L["prog"]) > 1]
+        assert joint and all(L["sd"] == sd for L in joint)
+        for _ in range(3):
+            fb.step_eager()
+        outs.append([ns.state() for ns in solvers])
+    for a, b in zip(*outs):
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
 
 
 RK3_CASES = [("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
