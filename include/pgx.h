@@ -82,7 +82,8 @@ enum pgx_opcode {
   PGX_OP_STENCIL_T = 12,/* slot a (N) = S^T slot a (N-2); mat: S[i+2,i]      */
   PGX_OP_TDMA2 = 13,    /* slots a..a+b-1 = (S^T S)^-1 slot; mat: (a,rden,w) per i */
   PGX_OP_DIFF = 14,     /* slots a..a+b-1 = D^k slot (Chebyshev recurrence)  */
-  PGX_OP_DCT = 15,      /* slot a = DCT-I slot a; k = mode; mat: twiddles    */
+  PGX_OP_DCT = 15,      /* slots a..a+b-1 (one length) = DCT-I of themselves, all slots through each
+                           phase together; k = mode; mat: twiddles */
   PGX_OP_BANDED = 17,   /* slot a = A slot a; k diagonals from offset b step 2, rows len; mat [k][rows] */
   PGX_OP_DENSE = 18,    /* slot a = A slot a; A is len x slen row-major       */
   PGX_OP_FDMA = 19,     /* in-place -2/0/+2/+4 LU solve of slots a..a+b-1, table mat+s: [l|dinv|u1|u2] */
