@@ -522,6 +522,42 @@ def run_adjoint(args, stream):
             "J": float(J[0]), "autotuned_adjoint_tiles": getattr(fa, "atuned", None)}
 
 
+def dense_dct_passes(f, c, g, axis, mma, st):
+    """c = Fwd f, g = Bwd c along ``axis`` (N x N, N lines) as LOAD / DENSE / STORE line programs with
+    the dense Chebyshev DCT matrices, the contraction on the FP64 tensor cores (``mma``) or as FMA
+    chains; 8 lines per CTA."""
+    import ctypes
+    from pypde_gb300 import _lib
+    from pypde_gb300._dev import to_dev
+    from pypde_gb300.navier.fused import dense_dct_host
+    N = f.shape[0]
+    mats = dense_dct_host(N)
+    keep = [to_dev(mats["dct_fwd"]), to_dev(mats["dct_bwd"])]
+    runs = []
+    for src, dst, A in ((f, c, keep[0]), (c, g, keep[1])):
+        P = _lib.PgxProgram()
+        P.axis, P.lines_len, P.tb, P.lcap, P.nslots, P.fft_n, P.nthreads = axis, 1, 8, (N + 1) | 1, 1, 0, 256
+        ops = [_lib.op("LOAD", a=0, arr=0, len=0), _lib.op("DENSE", a=0, mat=0, len=0, k=_lib.DENSE_MMA if mma else 0),
+               _lib.op("STORE", a=0, arr=1)]
+        P.nops = len(ops)
+        for i, o in enumerate(ops):
+            P.ops[i] = o
+        inst = _lib.PgxInstance()
+        for i, t in enumerate((src, dst)):
+            inst.arr[i].ptr, inst.arr[i].s0, inst.arr[i].s1 = t.data_ptr(), t.stride(0), t.stride(1)
+            inst.arr[i].n0, inst.arr[i].n1 = t.shape
+        inst.mat[0] = A.data_ptr()
+        inst.len[0], inst.len[1] = N, N
+        runs.append((P, inst))
+    L = _lib.lib()
+
+    def run():
+        for P, inst in runs:
+            _lib.check(L.pgx_run(ctypes.byref(P), ctypes.byref(inst), st), "dense dct")
+    run.keep = keep
+    return run
+
+
 def run_microbench(args):
     """Kernel microbench (seed 1): DCT-I forward + backward along each axis of N x N fields,
     N = 33 ... 1025, and the ADI Helmholtz solve (I - 0.01 Laplacian) u = f with Dirichlet bases
@@ -554,6 +590,16 @@ def run_microbench(args):
             flops = 2 * 2.5 * N * np.log2(2 * (N - 1)) * N
             row["axis%d" % axis] = {"ms_fwd_bwd": round(t, 5), "roundtrip_err": err,
                                     "tflops": round(flops / (t * 1e-3) / 1e12, 4)}
+            # the same transforms as dense matrices: tensor cores (DMMA) and FMA chains
+            for mma in (True, False):
+                fb2 = dense_dct_passes(f, c, g, axis, mma, st)
+                for _ in range(3):
+                    fb2()
+                t2 = statistics.median(time_steps(fb2, max(args.steps, 5), stream))
+                err2 = float((g - f).abs().max() / f.abs().max())
+                row["axis%d" % axis]["dense_mma" if mma else "dense_fma"] = {
+                    "ms_fwd_bwd": round(t2, 5), "roundtrip_err": err2,
+                    "tflops": round(2 * 2.0 * N * N * N / (t2 * 1e-3) / 1e12, 4)}
         dct.append(row)
     hh = []
     for N in (257, 1025):

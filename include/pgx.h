@@ -103,6 +103,9 @@ enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_F
  * warp per (line, parity) chain with a warp-parallel scan instead of one thread
  * per chain (for passes with few lines). */
 #define PGX_CHAIN_WARP 1
+/* op.k of DENSE: PGX_DENSE_MMA runs the contraction on the FP64 tensor cores (DMMA,
+ * 8 x 8 x 4 tiles: rows x lines x columns) instead of one FMA chain per output. */
+#define PGX_DENSE_MMA 2
 typedef struct pgx_op {
   int16_t code, a, b, arr, mat, len, par, k;
   double alpha;                    /* scalar; multiplied by par[par] when par >= 0 */

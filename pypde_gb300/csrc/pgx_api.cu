@@ -59,6 +59,11 @@ static int smem_optin_max() {
   return v;
 }
 
+// Longest DCT length run as a dense contraction on the FP64 tensor cores (and the longest
+// dense operator for which DMMA beats FMA chains on GB300, whose FP64 tensor rate is below
+// its DFMA rate).
+static const int DENSE_MMA_MAX_N = 33;
+
 static int check_program(const pgx_program* P) {
   if (!P) return PGX_E_ARG;
   if (P->axis < 0 || P->axis > 1 || P->tb < 1 || P->lcap < 1 || P->lcap > PGX_LMAX + 8) return PGX_E_ARG;
@@ -365,18 +370,32 @@ int pgx_dct_pass(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, d
   I.mat[0] = tab;
   P.nops = 3;
   P.ops[0] = mk(PGX_OP_LOAD, 0, -1, 0, -1, 1);
+  const bool mma = !fft && n <= DENSE_MMA_MAX_N;
   if (fft) {
     P.ops[1] = mk(PGX_OP_DCT, 0, -1, -1, 0, -1, mode);
     P.fft_n = n;
   } else {
-    P.ops[1] = mk(PGX_OP_DENSE, 0, -1, -1, 0, 1);
+    P.ops[1] = mk(PGX_OP_DENSE, 0, -1, -1, 0, 1, mma ? PGX_DENSE_MMA : 0);
   }
   P.ops[2] = mk(PGX_OP_STORE, 0, -1, 1);
   pick_tile(&P, nlines, n, 2, P.fft_n);
+  if (mma) {  // one 8-line tensor-core tile per CTA, a warp per 8-row block
+    P.tb = 8;
+    P.nthreads = 32 * ((n + 7) / 8);
+  }
   return pgx_run(&P, &I, stream);
 }
 
 bool pgx_fft_length_ok(int n) { return fft_length_ok(2 * (n - 1)); }
+
+// FFT or dense matrix for a DCT pass of `nlines` lines of length n.  Measured on GB300
+// (fwd + bwd along one axis of an N x N field): the dense contraction on the FP64 tensor
+// cores beats the FFT at N = 33 (latency: two phases instead of nine) and loses from N = 65
+// on (1.7x at 65, 18x at 1025); for many lines the FFT's 3-4x fewer FP64 operations win.
+static bool dct_use_fft(int n, int nlines) {
+  if (!fft_length_ok(2 * (n - 1))) return false;
+  return !(n <= DENSE_MMA_MAX_N && nlines <= 8 * 152);
+}
 
 extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t n_in, double* out, int64_t out_s0,
                         int64_t out_s1, int32_t n_out, int32_t n, int32_t nlines, int32_t axis, int32_t mode,
@@ -385,7 +404,7 @@ extern "C" int pgx_dct1(const double* in, int64_t in_s0, int64_t in_s1, int32_t 
       axis < 0 || axis > 1 || mode < 0 || mode > 4)
     return PGX_E_ARG;
   const double* tab = nullptr;
-  bool fft = fft_length_ok(2 * (n - 1));
+  bool fft = dct_use_fft(n, nlines);
   int rc = fft ? twiddles(n, &tab) : dense_dct(n, mode, &tab);
   if (rc) return rc;
   return pgx_dct_pass(in, in_s0, in_s1, n_in, out, out_s0, out_s1, n_out, n, nlines, axis, mode, tab, fft, stream);
@@ -402,7 +421,7 @@ extern "C" int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in
   if (work_doubles < (int64_t)n0_out * n1_in) return PGX_E_ARG;
   const double* t0 = nullptr;
   const double* t1 = nullptr;
-  bool f0 = fft_length_ok(2 * (N0 - 1)), f1 = fft_length_ok(2 * (N1 - 1));
+  bool f0 = dct_use_fft(N0, n1_in), f1 = dct_use_fft(N1, n0_out);
   int rc = f0 ? twiddles(N0, &t0) : dense_dct(N0, mode, &t0);
   if (!rc) rc = f1 ? twiddles(N1, &t1) : dense_dct(N1, mode, &t1);
   if (rc) return rc;

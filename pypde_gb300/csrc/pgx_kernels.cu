@@ -635,7 +635,61 @@ __device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   c.slen[op.a] = rows;
 }
 
+// D (8x8) += A (8x4, row-major) B (4x8, column-major) on the FP64 tensor cores; per lane
+// (g = lane / 4, q = lane % 4): a = A[g][q], b = B[q][g], d0, d1 = D[g][2q], D[g][2q+1].
+__device__ __forceinline__ void dmma_8x8x4(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+// y = A x per line on the tensor cores: Y (rows x tb) = A (rows x cols) X (cols x tb), one warp per
+// 8-row x 8-line output block, two accumulators over alternating column quads.
+__device__ void op_dense_mma(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const double* A = I.mat[op.mat];
+  const int rows = I.len[op.len];
+  const int cols = c.slen[op.a];
+  const double* x = slot_ptr(c, op.a);
+  double* y = spare_ptr(c);
+  zero_tail(c, y, rows);
+  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const int nrb = (rows + 7) >> 3, nlb = (c.tb + 7) >> 3;
+  for (int blk = warp; blk < nrb * nlb; blk += nw) {  // warp-uniform loop
+    const int lb = blk / nrb, rb = blk - lb * nrb;
+    const int r = rb * 8 + g, t = lb * 8 + g;          // the A row / X line this lane loads
+    const bool rok = r < rows, tok = t < c.tb;
+    const double* Ar = A + (size_t)(rok ? r : 0) * cols;
+    const double* xl = x + (tok ? t : 0) * c.lcap;
+    double d0 = 0.0, d1 = 0.0, e0 = 0.0, e1 = 0.0;
+    int k = 0;
+    for (; k + 8 <= cols; k += 8) {
+      const double a0 = rok ? __ldg(Ar + k + q) : 0.0, b0 = tok ? xl[k + q] : 0.0;
+      const double a1 = rok ? __ldg(Ar + k + 4 + q) : 0.0, b1 = tok ? xl[k + 4 + q] : 0.0;
+      dmma_8x8x4(d0, d1, a0, b0);
+      dmma_8x8x4(e0, e1, a1, b1);
+    }
+    for (; k < cols; k += 4) {
+      const bool kok = k + q < cols;
+      const double a0 = (rok && kok) ? __ldg(Ar + k + q) : 0.0, b0 = (tok && kok) ? xl[k + q] : 0.0;
+      dmma_8x8x4(d0, d1, a0, b0);
+    }
+    const int orow = rb * 8 + g, t0 = lb * 8 + 2 * q;
+    if (orow < rows) {
+      if (t0 < c.tb) y[t0 * c.lcap + orow] = d0 + e0;
+      if (t0 + 1 < c.tb) y[(t0 + 1) * c.lcap + orow] = d1 + e1;
+    }
+  }
+  __syncthreads();
+  swap_spare(c, op.a);
+  c.slen[op.a] = rows;
+}
+
 __device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  if (op.k & PGX_DENSE_MMA) {
+    op_dense_mma(c, op, I);
+    return;
+  }
   const double* A = I.mat[op.mat];
   const int rows = I.len[op.len];
   const int cols = c.slen[op.a];

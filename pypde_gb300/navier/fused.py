@@ -118,6 +118,7 @@ class Prog:
         or ``count`` dense-matrix ops."""
         self.has_dct = True
         if fft:
+            self._m(self._DENSE_DCT[mode])  # the dense form, for launches that contract on tensor cores
             self.add("DCT", s, b=count, mat="dct", k=mode)
         else:
             for i in range(count):
@@ -559,12 +560,25 @@ def dense_dct_host(n):
             "dct_fwd_t": np.ascontiguousarray(fwd.T)}
 
 
+_DENSE_DCT_CACHE = {}
+
+
+def _dense_dct_tables(n):
+    """Dense DCT matrices of length n on the current device, shared by every instance."""
+    key = (torch.cuda.current_device(), n)
+    if key not in _DENSE_DCT_CACHE:
+        _DENSE_DCT_CACHE[key] = {k: to_dev(v) for k, v in dense_dct_host(n).items()}
+    return _DENSE_DCT_CACHE[key]
+
+
 def _dct_tables(n, fft):
+    """Twiddles of the FFT-based DCT op (``fft``) and the dense matrices of the DENSE form."""
+    t = dict(_dense_dct_tables(n))
     if fft:
         h = ctypes.c_void_p()
         _lib.check(_lib.lib().pgx_dct_table(n, ctypes.byref(h)), "dct table")
-        return {"dct": h.value}
-    return {k: to_dev(v) for k, v in dense_dct_host(n).items()}
+        t["dct"] = h.value
+    return t
 
 
 def host_tables(N, M, tk, dt, nu, kappa, scale, fd, adjoint=False):
@@ -826,7 +840,7 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     wc = chains and width * lines_total < 152 * 64
     if wc:
         nt = max(256, min(1024, 32 * width * tb))
-    return tb, min(nt, 1024), bool(wc), sd
+    return tb, min(nt, 1024), bool(wc), sd, False
 
 
 def _candidates(prog, lines_total, lcap, fft_n, max_lines):
@@ -835,11 +849,19 @@ def _candidates(prog, lines_total, lcap, fft_n, max_lines):
     multi-slot DCT ops also with the DCTs one slot at a time (smaller FFT buffers)."""
     out = []
     for sd in ((False, True) if _fft_slots(prog) > 1 and fft_n > 1 else (False,)):
-        out += _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd)
+        out += _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, False)
+    if _has_dense(prog, fft_n):  # transforms / dense operators as tensor-core contractions
+        out += _candidates_sd(prog, lines_total, lcap, 0, max_lines, False, True)
     return out
 
 
-def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd):
+def _has_dense(prog, fft_n):
+    """Whether a launch of ``prog`` has contractions the tensor cores can run (DENSE ops, or
+    DCT ops whose dense matrices the program carries)."""
+    return any(o.code == _lib.OP["DENSE"] or (o.code == _lib.OP["DCT"] and fft_n > 1) for o in prog.ops)
+
+
+def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, dm):
     nbuf = prog.nslots + 1
     per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
     width = 1
@@ -851,8 +873,8 @@ def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd):
     tbs = set()
     for ctas in (1, 2, 3, 4):
         tb = (SMEM_PER_SM // ctas - 2048) // per_line
-        tbs.add(int(tb))
-    tbs.update({1, 2, 4, 8, 16})
+        tbs.add(int(tb) - int(tb) % 8 if dm and tb >= 8 else int(tb))
+    tbs.update({8, 16, 32} if dm else {1, 2, 4, 8, 16})  # tensor-core tiles are 8 lines wide
     chains = any(o.code in _CHAIN_CODES for o in prog.ops)
     out = []
     for tb in sorted(tbs):
@@ -863,14 +885,34 @@ def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd):
             continue
         for nt in (256, 512):
             nt = max(nt, 32 * -(-width * tb // 32))
-            if nt <= 1024 and (tb, nt, False, sd) not in out:
-                out.append((tb, nt, False, sd))
+            if nt <= 1024 and (tb, nt, False, sd, dm) not in out:
+                out.append((tb, nt, False, sd, dm))
         if chains:  # warp-per-chain variants: a warp for each of the CTA's chains, up to 1024 threads
             for nt in (256, min(1024, 32 * width * tb)):
                 nt = max(nt, 256)
-                if nt <= 1024 and (tb, nt, True, sd) not in out:
-                    out.append((tb, nt, True, sd))
+                if nt <= 1024 and (tb, nt, True, sd, dm) not in out:
+                    out.append((tb, nt, True, sd, dm))
     return out
+
+
+def launch_ops(prog, sd=False, dm=False):
+    """The ops of one launch of ``prog``: with ``sd`` each multi-slot DCT op becomes one op per
+    slot; with ``dm`` each DCT op becomes dense-matrix ops (the program carries the matrices)
+    and every DENSE op runs on the FP64 tensor cores."""
+    ops = []
+    for o in prog.ops:
+        if dm and o.code == _lib.OP["DCT"]:
+            mat = prog.mats[Prog._DENSE_DCT[o.k]]
+            ops += [_lib.op("DENSE", a=o.a + i, mat=mat, len=L_ND + prog.axis, k=_lib.DENSE_MMA)
+                    for i in range(max(o.b, 1))]
+        elif dm and o.code == _lib.OP["DENSE"]:
+            ops.append(_lib.op("DENSE", a=o.a, b=o.b, arr=o.arr, mat=o.mat, len=o.len,
+                               k=o.k | _lib.DENSE_MMA, alpha=o.alpha, par=o.par))
+        elif sd and o.code == _lib.OP["DCT"] and o.b > 1:
+            ops += [_lib.op("DCT", a=o.a + i, b=1, mat=o.mat, k=o.k) for i in range(o.b)]
+        else:
+            ops.append(o)
+    return ops
 
 
 class FusedBatch:
@@ -945,16 +987,14 @@ class FusedBatch:
                 I.fill(prog, insts[k * nv + v], stage, var)
         return torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
 
-    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None, sd=False):
+    def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None, sd=False, dm=False):
         """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode;
-        ``sd``: multi-slot DCT ops as one op per slot."""
+        ``sd``: multi-slot DCT ops as one op per slot; ``dm``: DCT ops as dense matrices and every
+        DENSE op on the FP64 tensor cores (no FFT buffers)."""
         lcap, fft_n = key
-        ops = []
-        for o in prog.ops:
-            if sd and o.code == _lib.OP["DCT"] and o.b > 1:
-                ops += [_lib.op("DCT", a=o.a + i, b=1, mat=o.mat, k=o.k) for i in range(o.b)]
-            else:
-                ops.append(o)
+        ops = launch_ops(prog, sd, dm)
+        if dm:
+            fft_n = 0
         P = _lib.PgxProgram()
         P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
         P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), fft_n, nt
@@ -968,7 +1008,7 @@ class FusedBatch:
                 for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
         return {"name": name or prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
-                "key": key, "members": members, "prog": prog, "wc": bool(wc), "sd": bool(sd)}
+                "key": key, "members": members, "prog": prog, "wc": bool(wc), "sd": bool(sd), "dm": bool(dm)}
 
     def _pass_launches(self, prog, tiles=None, stage=0):
         d_insts = self._d_insts(prog, stage)
@@ -978,10 +1018,10 @@ class FusedBatch:
             lines = [self.insts[k].lines(prog) for k in members]
             tag = "%s#%d" % (name, gi)
             if tiles and tag in tiles:
-                tb, nt, wc, sd = (tuple(tiles[tag][:4]) + (False, False))[:4]
+                tb, nt, wc, sd, dm = (tuple(tiles[tag][:5]) + (False,) * 3)[:5]
             else:
-                tb, nt, wc, sd = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
-            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, bool(wc), name, bool(sd)))
+                tb, nt, wc, sd, dm = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
+            out.append(self._group_launch(prog, d_insts, key, members, tb, nt, bool(wc), name, bool(sd), bool(dm)))
         return out
 
     def _build_launches(self, tiles=None):
@@ -991,7 +1031,7 @@ class FusedBatch:
 
     @staticmethod
     def _tiles_of(launch_sets):
-        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads, L["wc"], L["sd"])
+        return {"%s#%d" % (L["name"], gi): (L["P"].tb, L["P"].nthreads, L["wc"], L["sd"], L["dm"])
                 for group in launch_sets for gi, L in enumerate(group)}
 
     def tiles(self):
@@ -1016,8 +1056,9 @@ class FusedBatch:
                 prog, key, members = L0["prog"], L0["key"], L0["members"]
                 lines = [self.insts[k].lines(prog) for k in members]
                 best = None
-                for tb, nt, wc, sd in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines)):
-                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"], sd)
+                for tb, nt, wc, sd, dm in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1],
+                                                      max(lines)):
+                    L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"], sd, dm)
                     self._run_launch(L)
                     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -1027,11 +1068,11 @@ class FusedBatch:
                     torch.cuda.synchronize()
                     ms = a.elapsed_time(b) / reps
                     if verbose:
-                        print(prog.name, gi, tb, nt, wc, sd, round(ms, 4))
+                        print(prog.name, gi, tb, nt, wc, sd, dm, round(ms, 4))
                     if best is None or ms < best[0]:
-                        best = (ms, L, tb, nt, wc, sd)
+                        best = (ms, L, tb, nt, wc, sd, dm)
                 group[gi] = best[1]
-                chosen["%s#%d" % (L0["name"], gi)] = (best[2], best[3], best[4], best[5], round(best[0], 4))
+                chosen["%s#%d" % (L0["name"], gi)] = best[2:] + (round(best[0], 4),)
         return chosen
 
     def autotune(self, reps=3, verbose=False):

@@ -168,3 +168,30 @@ def test_adjoint_of_split_form_is_the_transpose(tk):
         m.run(p)
     rhs = sum(float((m.arrays["b" + k] * d[k]).sum()) for k in STATE)
     assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)
+
+
+@pytest.mark.parametrize("sd,dm", [(True, False), (False, True)], ids=["per-slot-dct", "dense-mma"])
+def test_launch_rewrites_give_the_same_step(sd, dm):
+    """The per-launch op rewrites (multi-slot DCT ops split per slot; DCT ops as the program's dense
+    matrices on the tensor cores) compute the same forward and reverse-mode passes."""
+    import copy
+    from pypde_gb300.navier.fused import launch_ops
+    m, rng = make_machine(12, 13, "CN", True, 4)
+    progs = build_programs("CN", True) + build_adjoint_programs("CN", True)
+    X = {k: 1e-1 * rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    G = {k: rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    out = []
+    for rewrite in (False, True):
+        for k in STATE:
+            m.arrays[k][...] = X[k]
+            m.arrays["b" + k][...] = G[k]
+        m.arrays["bPG"][...] = 0.0
+        for p in progs:
+            if rewrite:
+                p = copy.copy(p)
+                p.ops = launch_ops(p, sd, dm)
+            m.run(p)
+        out.append({k: m.arrays[k].copy() for k in STATE + tuple("b" + k for k in STATE)})
+    for k in out[0]:
+        scale = np.abs(out[0][k]).max()
+        assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * scale, k

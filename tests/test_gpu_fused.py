@@ -144,7 +144,7 @@ def test_warp_parallel_chains_match_sequential(NS):
             solvers.append(ns)
         fb = FusedBatch(solvers)
         tiles = {}
-        for tag, (tb, nt, wc, sd) in fb.tiles().items():
+        for tag, (tb, nt, wc, sd, dm) in fb.tiles().items():
             prog = fb.progs[[p.name for p in fb.progs].index(tag.split("#")[0])]
             chains = any(o.code in _CHAIN_CODES for o in prog.ops)
             tiles[tag] = (tb, max(nt, 256), warp and chains)
@@ -173,7 +173,7 @@ def test_joint_and_serial_dct_ops_agree(NS):
             solvers.append(ns)
         fb = FusedBatch(solvers)
         assert fb.fft
-        tiles = {tag: (tb, nt, wc, sd) for tag, (tb, nt, wc, _) in fb.tiles().items()}
+        tiles = {tag: (tb, nt, wc, sd, dm) for tag, (tb, nt, wc, _, dm) in fb.tiles().items()}
         fb._build_launches(tiles)
         joint = [L for g in fb.launches for L in g if _fft_slots(L["prog"]) > 1]
         assert joint and all(L["sd"] == sd for L in joint)
@@ -183,6 +183,40 @@ def test_joint_and_serial_dct_ops_agree(NS):
     for a, b in zip(*outs):
         for k in a:
             assert np.array_equal(a[k], b[k]), k
+
+
+def test_tensor_core_contractions_match(NS):
+    """Launches whose DCT ops run as dense matrices and whose DENSE ops (the DCTs, H_y, Q_y) run on
+    the FP64 tensor cores (DMMA) give the FFT / FMA-chain step to rounding, and the oracle."""
+    from pypde_gb300.navier.fused import FusedBatch, _has_dense
+    specs = [((65, 33), 1e5, 1), ((33, 33), 1e4, 2), ((19, 33), 3e4, 3)]
+    outs = []
+    for dm in (False, True):
+        solvers = []
+        for shape, ra, seed in specs:
+            ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers)
+        tiles = {}
+        for gl in fb.launches:
+            for gi, L in enumerate(gl):
+                use = dm and _has_dense(L["prog"], L["key"][1])
+                tiles["%s#%d" % (L["name"], gi)] = (8 if use else L["P"].tb, max(L["P"].nthreads, 256), L["wc"],
+                                                    False, use)
+        fb._build_launches(tiles)
+        assert any(L["dm"] for g in fb.launches for L in g) == dm
+        if dm:
+            assert all(L["P"].fft_n == 0 for g in fb.launches for L in g if L["dm"])
+        for _ in range(3):
+            fb.step_eager()
+        outs.append([ns.state() for ns in solvers])
+    for a, b in zip(*outs):
+        for k in a:
+            assert rel_err(b[k], a[k]) < 1e-11, k
+    for ns, (shape, ra, seed) in zip(solvers, specs):
+        ref = oracle_run("linear", shape, dict(ra=ra, dt=0.005, dealias=True), seed, 1e-3, 3)
+        compare(ns, ref, 1e-8)
 
 
 RK3_CASES = [("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
