@@ -38,7 +38,7 @@ from ..host import fdma_lu, pseudoinverse_d2, stencil_matrix, stencil_sub
 # fixed len[] indices
 L_LINES, L_N, L_M, L_NG, L_MG, L_ND, L_MD = range(7)
 # fixed par[] indices
-P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT, P_B, P_C, P_TF = range(12)
+P_ISX, P_ISZ, P_MDT, P_DT, P_DTK, P_MDTSX, P_MDTSZ, P_MNU, P_IDT, P_B, P_C, P_TF, P_EDU, P_EDT = range(14)
 
 FFT_RADICES = (2, 3)
 
@@ -156,7 +156,7 @@ class Prog:
         self.add("TDMA2", s, b=count, mat="tdma_" + kind)
 
 
-def _split_convection_programs(tkind, fft, rk3):
+def _split_convection_programs(tkind, fft, rk3, beta=False):
     """P1, P2u, P2, P3, P3r with P1 / P2 / P3 written once for a generic field F (variants)."""
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
@@ -241,12 +241,44 @@ def _split_convection_programs(tkind, fft, rk3):
     p.store_add(0, "RHS_V")
     p.load(0, "DTB2", L_N, par=P_DTK)
     p.store_add(0, "RHS_T")
+    if beta:
+        p.nslots = 3
+        for F in "UVT":
+            _explicit_diffusion_x(p, 0, F, kinds[F])
+            p.store_add(0, "RHS_" + F, par=P_EDT if F == "T" else P_EDU)
     P.append(p)
     return P
 
 
-def build_programs(tkind, fft, rk3=False, split=False):
-    """The eleven passes of one IMEX Euler step (beta = 1).  ``tkind`` is the x-basis of T
+def _explicit_diffusion_y():
+    """P2e (y, lines N-2): S_y F and D_y^2 S_y F / sz^2 of the state, the y-halves of the explicit
+    diffusion (1 - beta) dt a nu (d_xx + d_zz) F of rbc2d.py:268-283 (x-halves in P3)."""
+    p = Prog("P2e", 1, L_NG, 1)
+    for F in "UVT":
+        p.load(0, F + "G", L_MG)
+        p.stencil(0, "CD")
+        p.store(0, "EY0_" + F)
+        p.diff(0, count=2)
+        p.scale(0, par=P_ISZ)
+        p.scale(0, par=P_ISZ)
+        p.store(0, "EYY_" + F)
+    return p
+
+
+def _explicit_diffusion_x(p, s, F, kind):
+    """Slot s = D_x^2 S_x EY0_F / sx^2 + S_x EYY_F (Chebyshev x Chebyshev); uses slot s + 1."""
+    p.load(s, "EY0_" + F, L_NG)
+    p.stencil(s, kind)
+    p.diff(s, count=2)
+    p.scale(s, par=P_ISX)
+    p.scale(s, par=P_ISX)
+    p.load(s + 1, "EYY_" + F, L_NG)
+    p.stencil(s + 1, kind)
+    p.axpy(s, s + 1)
+
+
+def build_programs(tkind, fft, rk3=False, split=False, beta=False):
+    """The eleven passes of one IMEX Euler step.  ``tkind`` is the x-basis of T
     ("CD" for the linear / zero cases, "CN" for rbc).
 
     ``rk3``: the passes of one stage of the three-stage IMEX Runge-Kutta step
@@ -260,13 +292,19 @@ def build_programs(tkind, fft, rk3=False, split=False):
     ``split``: P1 - P3 as per-field programs run as three descriptors of one launch
     (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3r (the non-convective
     right-hand-side terms): the same transforms in twelve passes, with three times
-    the CTAs in the transform-heavy ones - for batches of few instances."""
+    the CTAs in the transform-heavy ones - for batches of few instances.
+
+    ``beta``: diffusion beta-implicit (beta != 1, rbc2d.py:268-283, 390-391): the ADI tables and the
+    pressure update carry beta (per-instance tables and parameters), and an extra pass P2e with
+    additions to P3 (P3r in the per-field form) put the explicit part into the right-hand sides."""
     P = []
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
 
     if split:
-        P += _split_convection_programs(tkind, fft, rk3)
+        P += _split_convection_programs(tkind, fft, rk3, beta)
+        if beta:
+            P.insert(3, _explicit_diffusion_y())   # P1, P2u, P2, P2e, P3, P3r
     else:
         # P1 (x, lines M-2): physical-in-x parts of F and dF/dx
         p = Prog("P1", 0, L_MG, 2)
@@ -324,7 +362,9 @@ def build_programs(tkind, fft, rk3=False, split=False):
         P.append(p)
 
         # P3 (x, lines M): forward x-transform and right-hand sides
-        p = Prog("P3", 0, L_M, 4)
+        if beta:
+            P.append(_explicit_diffusion_y())
+        p = Prog("P3", 0, L_M, 5 if beta else 4)
         for i, F in enumerate("UVT"):
             p.load(i, "C_" + F, L_ND)
         p.dct(0, FWD, fft, count=3)
@@ -343,6 +383,9 @@ def build_programs(tkind, fft, rk3=False, split=False):
                 p.axpy(i, 3, par=P_DT)
             else:
                 p.load_add(i, "DTB2", par=P_DTK)
+            if beta:
+                _explicit_diffusion_x(p, 3, F, kinds[F])
+                p.axpy(i, 3, par=P_EDT if F == "T" else P_EDU)
             p.store(i, "RHS_" + F)
         P.append(p)
 
@@ -617,23 +660,29 @@ def host_tables(N, M, tk, dt, nu, kappa, scale, fd, adjoint=False):
     return t
 
 
-def instance_params(N, M, dealias, dt, nu, kappa, scale, a=1.0, b=1.0, c=0.0):
+def instance_params(N, M, dealias, dt, nu, kappa, scale, a=1.0, b=1.0, c=0.0, beta=1.0):
     """len[] and par[] of one instance (indices L_* and P_*) for the stage coefficients a, b, c
-    (IMEX Euler: 1, 1, 0)."""
+    (IMEX Euler: 1, 1, 0) and the implicit fraction ``beta`` of the diffusion."""
     Nd, Md = (int(1.5 * N), int(1.5 * M)) if dealias else (N, M)
     sx, sz = scale
     lens = [0, N, M, N - 2, M - 2, Nd, Md]
     da = dt * a
-    par = [1.0 / sx, 1.0 / sz, -dt, da, da * kappa, -da / sx, -da / sz, -nu, 1.0 / da, b, c, 0.0]
+    par = [1.0 / sx, 1.0 / sz, -dt, da, da * kappa, -da / sx, -da / sz, -nu * beta, 1.0 / da, b, c, 0.0,
+           da * (1.0 - beta) * nu, da * (1.0 - beta) * kappa]
     return lens, par
 
 
 A_KEYS = ("A_U0", "A_Ux", "A_V0", "A_Vx", "A_T0", "A_Tx")
 
 
-def scratch_shapes(N, M, Nd, Md):
-    """Intermediate arrays of the forward passes (name -> shape)."""
+def scratch_shapes(N, M, Nd, Md, beta=False):
+    """Intermediate arrays of the forward passes (name -> shape); ``beta``: with those of the
+    explicit diffusion (beta != 1)."""
     sh = {}
+    if beta:
+        for F in "UVT":
+            sh["EY0_" + F] = (N - 2, M)
+            sh["EYY_" + F] = (N - 2, M)
     for F in "UVT":
         sh["A_" + F + "0"] = (Nd, M - 2)
         sh["A_" + F + "x"] = (Nd, M - 2)
@@ -663,10 +712,9 @@ class _Instance:
         return {"UG": (N - 2, M - 2), "VG": (N - 2, M - 2), "TG": (N - 2, M - 2), "PG": (N - 2, M - 2),
                 "PRES": (N, M)}
 
-    def __init__(self, ns, fft, views=None, bind=True):
-        if ns.nstage not in (1, 3) or ns.beta != 1.0:
-            raise NotImplementedError("the fused step covers IMEX Euler and RK3 with beta = 1; use update() "
-                                      "otherwise")
+    def __init__(self, ns, fft, views=None, bind=True, beta=False):
+        if ns.nstage not in (1, 3):
+            raise NotImplementedError("the fused step covers IMEX Euler and RK3; use update() otherwise")
         self.ns = ns
         N, M = ns.shape
         Nd, Md = (int(1.5 * N), int(1.5 * M)) if ns.dealias else (N, M)
@@ -687,14 +735,15 @@ class _Instance:
         a["TBCC"] = ns.Tbc_cheby.contiguous()
         a["DTB1"] = ns.dTbcdz1.contiguous()
         a["DTB2"] = ns.dTbcdz2.contiguous()
-        for k, shp in scratch_shapes(N, M, Nd, Md).items():
+        for k, shp in scratch_shapes(N, M, Nd, Md, beta).items():
             a[k] = views[k] if (views is not None and k in views) else z(*shp)
         self.arrays = a
-        self.lens, self.par = instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale)
+        bt = float(ns.beta)
+        self.lens, self.par = instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale, beta=bt)
         # operator tables
         g = _global_tables()
         t = {"sten_CD": g["sten_CD"], "sten_CN": g["sten_CN"], "tdma_CD": g["tdma_CD"]}
-        host = host_tables(N, M, ns.T.xs[0].id, ns.dt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
+        host = host_tables(N, M, ns.T.xs[0].id, ns.dt * bt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
         t.update({k: to_dev(v) for k, v in host.items()})
         self.tables = t
         # per stage: parameters, ADI tables (lambda = dt a nu or dt a kappa) and the velocity arrays
@@ -708,8 +757,9 @@ class _Instance:
             for st in range(3):
                 ak, bk, ck = float(ns.a[st]), float(ns.b[st]), float(ns.c[st])
                 self.stage_par.append(instance_params(N, M, ns.dealias, ns.dt, ns.nu, ns.kappa, ns.scale,
-                                                      ak, bk, ck)[1])
-                hs = host_tables(N, M, ns.T.xs[0].id, ns.dt * ak, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd)
+                                                      ak, bk, ck, bt)[1])
+                hs = host_tables(N, M, ns.T.xs[0].id, ns.dt * ak * bt, ns.nu, ns.kappa, ns.scale,
+                                 ns.solver_P._fd)
                 self.stage_tables.append({k: to_dev(hs[k]) for k in ("Ax_U", "Ax_T", "Ay_U", "Ay_T")})
                 cur, old = ("A", "A") if st == 0 else (("B", "A") if st == 1 else ("A", "B"))
                 self.stage_arrays.append({"UXC": "UX_" + cur, "UZC": "UZ_" + cur, "UXO": "UX_" + old,
@@ -941,6 +991,9 @@ class FusedBatch:
                    for ns, nd in zip(self.solvers, sizes)]
         self.a_arena = torch.zeros(sum(r * c for sh in ashapes for (r, c) in sh.values()), dtype=DTYPE,
                                    device=device())
+        # explicit diffusion (beta != 1) in any instance: the batch runs the passes that carry it
+        # (instances with beta = 1 add zero)
+        self.beta = any(float(ns.beta) != 1.0 for ns in self.solvers)
         self.insts, off, aoff = [], 0, 0
         for ns, sh, ash in zip(self.solvers, shapes, ashapes):
             views = {}
@@ -951,14 +1004,14 @@ class FusedBatch:
             for key, (r, c) in ash.items():
                 views[key] = self.a_arena[aoff:aoff + r * c].view(r, c)
                 aoff += r * c
-            self.insts.append(_Instance(ns, self.fft, views, bind))
+            self.insts.append(_Instance(ns, self.fft, views, bind, self.beta))
         nst = {ns.nstage for ns in self.solvers}
         if len(nst) != 1:
             raise ValueError("all instances of a batch need the same integrator")
         self.nstage = nst.pop()
         self.tkind = tkinds.pop()
         self.split = len(self.solvers) <= self.SPLIT_MAX if split is None else bool(split)
-        self.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=self.split)
+        self.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=self.split, beta=self.beta)
         self._build_launches()
         self.graph = None
 
@@ -1128,8 +1181,8 @@ class FusedBatch:
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""
         one = FusedBatch.__new__(FusedBatch)
         one.solvers, one.insts, one.fft = [self.solvers[i]], [self.insts[i]], self.fft
-        one.nstage, one.tkind, one.split = self.nstage, self.tkind, True
-        one.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=True)
+        one.nstage, one.tkind, one.split, one.beta = self.nstage, self.tkind, True, self.beta
+        one.progs = build_programs(self.tkind, self.fft, rk3=self.nstage == 3, split=True, beta=self.beta)
         one.state_arena = None
         one._build_launches()
         one.graph = None

@@ -41,15 +41,45 @@ import torch
 
 from .. import _lib
 from .._dev import DTYPE, device, to_dev
-from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX, P_MDTSZ,
-                    P_MNU, P_TF, FusedBatch, Prog, _Instance, build_programs, host_tables)
+from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_EDT, P_EDU, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX,
+                    P_MDTSZ, P_MNU, P_TF, FusedBatch, Prog, _Instance, build_programs, host_tables)
 
 BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
 
-def build_adjoint_programs(tkind, fft, split=False):
-    """R1 and the thirteen transposed passes of one IMEX Euler step (beta = 1); R1 is the
-    forward P1 of the same form (``split``: per-field) as the batch's forward passes."""
+def _explicit_diffusion_x_t(p, s, F, kind, src):
+    """Transpose of the x-half of the explicit diffusion (P3): from the right-hand-side gradient
+    ``src``, EY0_F bar = P_ED S_x^T (D_x^T)^2 / sx^2 and EYY_F bar = P_ED S_x^T of it."""
+    ed = P_EDT if F == "T" else P_EDU
+    p.load(s, src, L_N, par=ed)
+    p.stencil_t(s, kind)
+    p.store(s, "bEYY_" + F)
+    p.load(s, src, L_N, par=ed)
+    p.scale(s, par=P_ISX)
+    p.scale(s, par=P_ISX)
+    p.diff_t(s, count=2)
+    p.stencil_t(s, kind)
+    p.store(s, "bEY0_" + F)
+
+
+def _explicit_diffusion_y_t():
+    """Q2e (y, N-2 lines), the transpose of P2e: F bar += S_y^T EY0_F bar + S_y^T (D_y^T)^2 EYY_F bar / sz^2."""
+    p = Prog("Q2e", 1, L_NG, 1)
+    for F in "UVT":
+        p.load(0, "bEYY_" + F, L_M)
+        p.scale(0, par=P_ISZ)
+        p.scale(0, par=P_ISZ)
+        p.diff_t(0, count=2)
+        p.load_add(0, "bEY0_" + F)
+        p.stencil_t(0, "CD")
+        p.store_add(0, "b" + F + "G")
+    return p
+
+
+def build_adjoint_programs(tkind, fft, split=False, beta=False):
+    """R1 and the thirteen transposed passes of one IMEX Euler step; R1 is the forward P1 of
+    the same form (``split``: per-field) as the batch's forward passes.  ``beta``: with the
+    transposes of the explicit-diffusion terms (Q3 / Q3r and the extra pass Q2e)."""
     BWD, BWD_T, FWD_T = _lib.DCT_BWD, _lib.DCT_BWD_T, _lib.DCT_FWD_T
     kinds = {"U": "CD", "V": "CD", "T": tkind}
     ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
@@ -181,10 +211,15 @@ def build_adjoint_programs(tkind, fft, split=False):
         p.load(0, "bRHS_V", L_N, par=P_DT)
         p.stencil_t(0, tkind)
         p.store(0, "bTSY")
+        if beta:
+            for F in "UVT":
+                _explicit_diffusion_x_t(p, 0, F, kinds[F], "bRHS_" + F)
         Q.append(p)
     else:
         p = Prog("Q3", 0, L_M, 4)
         for i, F in enumerate("UVT"):
+            if beta:
+                _explicit_diffusion_x_t(p, 3, F, kinds[F], "bRHS_" + F)
             p.load(i, "bRHS_" + F, L_N)
             if F == "U":
                 p.copy(3, i)
@@ -205,6 +240,9 @@ def build_adjoint_programs(tkind, fft, split=False):
         for i, F in enumerate("UVT"):
             p.store(i, "bC_" + F)
         Q.append(p)
+
+    if beta:
+        Q.append(_explicit_diffusion_y_t())
 
     # Q2u / Q2f / Q2z (y, Nd lines): C = Fwd_y(dF/dx ux + dF/dz uz [+ DTB1 uz]), linearised.
     # Q2f runs once per field (three descriptors of one program, "variants"), so one instance
@@ -293,9 +331,13 @@ def build_adjoint_programs(tkind, fft, split=False):
     return Q
 
 
-def adjoint_shapes(N, M, Nd, Md):
+def adjoint_shapes(N, M, Nd, Md, beta=False):
     """Intermediate arrays of the adjoint passes (name -> shape)."""
     sh = {}
+    if beta:
+        for F in "UVT":
+            sh["bEY0_" + F] = (N - 2, M)
+            sh["bEYY_" + F] = (N - 2, M)
     for k in ("bUS", "bVS", "bX", "bR2"):
         sh[k] = (N - 2, M - 2)
     for k in ("bG1", "bG2", "bY1", "bY2", "bW1", "bW2", "bR1", "bTSY"):
@@ -313,7 +355,7 @@ def adjoint_shapes(N, M, Nd, Md):
     return sh
 
 
-def add_adjoint_buffers(I, bar_views):
+def add_adjoint_buffers(I, bar_views, beta=False):
     """Gradient arrays, scratch and transposed operator tables of one instance."""
     ns = I.ns
     N, M, Nd, Md = I.N, I.M, I.Nd, I.Md
@@ -321,9 +363,10 @@ def add_adjoint_buffers(I, bar_views):
     a = I.arrays
     for k in BAR_STATE:
         a[k] = bar_views[k]
-    for k, shp in adjoint_shapes(N, M, Nd, Md).items():
+    for k, shp in adjoint_shapes(N, M, Nd, Md, beta).items():
         a[k] = torch.zeros(shp, dtype=DTYPE, device=dev)
-    host = host_tables(N, M, ns.T.xs[0].id, ns.dt, ns.nu, ns.kappa, ns.scale, ns.solver_P._fd, adjoint=True)
+    host = host_tables(N, M, ns.T.xs[0].id, ns.dt * float(ns.beta), ns.nu, ns.kappa, ns.scale, ns.solver_P._fd,
+                       adjoint=True)
     for k in ("BxT", "ByT", "BSx_UT", "BSx_TT", "BSyT", "HyT", "QyT"):
         I.tables[k] = to_dev(host[k])
 
@@ -349,9 +392,9 @@ class FusedAdjoint(FusedBatch):
                 r, c = I.arrays[key].shape
                 views["b" + key] = self.bar_arena[off:off + r * c].view(r, c)
                 off += r * c
-            add_adjoint_buffers(I, views)
+            add_adjoint_buffers(I, views, self.beta)
         tkind = self.solvers[0].T.xs[0].id
-        self.aprogs = build_adjoint_programs(tkind, self.fft, self.split)
+        self.aprogs = build_adjoint_programs(tkind, self.fft, self.split, self.beta)
         self.alaunches = [self._pass_launches(p) for p in self.aprogs]
         self.agraph = None
 

@@ -96,8 +96,8 @@ class NavierStokesSteadyState:
     def solve_steady_state(self, X0=None, dt=None, maxiter=300, disp=True, tol=1e-8,
                            jac_options={"inner_maxiter": 30}):  # noqa: B006 (the reference's signature)
         """Newton-Krylov for F = 0 (rbc2d_base.py:266-294); ``tol`` bounds max|F| like scipy's fatol."""
-        if self.nstage != 1 or self.beta != 1.0:
-            raise NotImplementedError("the fused residual covers IMEX Euler with beta = 1")
+        if self.nstage != 1:
+            raise NotImplementedError("the fused residual covers IMEX Euler")
         nsteps = 1 if dt is None else int(round(dt / self.dt))
         dt = self.dt if dt is None else dt
         m = int(jac_options.get("inner_maxiter", 30))

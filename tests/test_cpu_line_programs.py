@@ -18,11 +18,11 @@ from pypde_gb300.templates import poisson2d_matrices
 STATE = ("UG", "VG", "TG", "PRES")
 
 
-def make_machine(N, M, tk, dealias, seed):
+def make_machine(N, M, tk, dealias, seed, beta=1.0):
     rng = np.random.default_rng(seed)
     ra, pr, dt, aspect = 3e4, 1.0, 0.01, 1.5
     nu, kappa, scale = np.sqrt(pr / ra), np.sqrt(1.0 / pr / ra), (aspect * 0.5, 0.5)
-    lens, par = instance_params(N, M, dealias, dt, nu, kappa, scale)
+    lens, par = instance_params(N, M, dealias, dt, nu, kappa, scale, beta=beta)
     Nd, Md = lens[5], lens[6]
 
     def mats(n):
@@ -30,8 +30,8 @@ def make_machine(N, M, tk, dealias, seed):
 
     fd = poisson2d_matrices(mats(N), mats(M), True, scale)
     tables = global_tables_host()
-    tables.update(host_tables(N, M, tk, dt, nu, kappa, scale, fd, adjoint=True))
-    shapes = {**scratch_shapes(N, M, Nd, Md), **adjoint_shapes(N, M, Nd, Md)}
+    tables.update(host_tables(N, M, tk, dt * beta, nu, kappa, scale, fd, adjoint=True))
+    shapes = {**scratch_shapes(N, M, Nd, Md, beta != 1.0), **adjoint_shapes(N, M, Nd, Md, beta != 1.0)}
     for k in ("UG", "VG", "TG", "PG"):
         shapes[k] = shapes["b" + k] = (N - 2, M - 2)
     shapes["PRES"] = shapes["bPRES"] = (N, M)
@@ -195,3 +195,72 @@ def test_launch_rewrites_give_the_same_step(sd, dm):
     for k in out[0]:
         scale = np.abs(out[0][k]).max()
         assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * scale, k
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["fused", "per-field"])
+@pytest.mark.parametrize("tk", ["CD", "CN"])
+def test_beta_programs(tk, split):
+    """beta != 1: the explicit-diffusion passes give the plain-path step's diffusion term (against
+    the same programs with beta = 1 plus the term computed densely), and the reverse-mode passes
+    stay the exact transpose."""
+    from pypde_gb300.host import stencil_matrix as S
+    beta = 0.6
+    m, rng = make_machine(12, 13, tk, True, 5, beta)
+    fwd = build_programs(tk, True, split=split, beta=True)
+    adj = build_adjoint_programs(tk, True, split=split, beta=True)
+    names = [p.name for p in fwd]
+    assert "P2e" in names and names.index("P2e") < names.index("P3")
+    # the x- and y-halves written into the right-hand sides: compare with dense operators
+    X = {k: 1e-1 * rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    for k in STATE:
+        m.arrays[k][...] = X[k]
+    for p in fwd:
+        if p.name in ("P2e",):
+            m.run(p)
+    N, M = 12, 13
+    sx, sz = 1.5 * 0.5, 0.5
+    Dn, Dm = cheb_diff_matrix(N), cheb_diff_matrix(M)
+    for F, kind in (("U", "CD"), ("T", tk)):
+        Sx, Sy = S(kind, N), S("CD", M)
+        ref0 = X[F + "G"] @ Sy.T
+        refyy = X[F + "G"] @ (Dm @ Dm @ Sy).T / sz ** 2
+        assert np.allclose(m.arrays["EY0_" + F], ref0, atol=1e-12 * np.abs(ref0).max())
+        assert np.allclose(m.arrays["EYY_" + F], refyy, atol=1e-12 * np.abs(refyy).max())
+        del Sx
+    # exact transpose of the whole step
+    d = {k: rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    g = {k: rng.standard_normal(m.arrays[k].shape) for k in STATE}
+
+    def phi(Y):
+        for k in STATE:
+            m.arrays[k][...] = Y[k]
+        for p in fwd:
+            m.run(p)
+        return {k: m.arrays[k].copy() for k in STATE}
+
+    h = 1e-3
+    yp = phi({k: X[k] + h * d[k] for k in STATE})
+    ym = phi({k: X[k] - h * d[k] for k in STATE})
+    lhs = sum(float((g[k] * (yp[k] - ym[k])).sum()) / (2 * h) for k in STATE)
+    for k in STATE:
+        m.arrays[k][...] = X[k]
+        m.arrays["b" + k][...] = g[k]
+    m.arrays["bPG"][...] = 0.0
+    for p in adj:
+        m.run(p)
+    rhs = sum(float((m.arrays["b" + k] * d[k]).sum()) for k in STATE)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)
+
+
+def test_beta_split_matches_fused():
+    m, rng = make_machine(11, 13, "CN", True, 6, 0.5)
+    X = {k: 1e-1 * rng.standard_normal(m.arrays[k].shape) for k in STATE}
+    out = []
+    for split in (False, True):
+        for k in STATE:
+            m.arrays[k][...] = X[k]
+        for p in build_programs("CN", True, split=split, beta=True):
+            m.run(p)
+        out.append({k: m.arrays[k].copy() for k in STATE})
+    for k in STATE:
+        assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * np.abs(out[0][k]).max(), k

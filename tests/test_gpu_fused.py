@@ -219,6 +219,65 @@ def test_tensor_core_contractions_match(NS):
         compare(ns, ref, 1e-8)
 
 
+BETA_CASES = [
+    ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True, integrator="eu", beta=0.5), None),
+    ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True, integrator="eu", beta=0.5), False),
+    ("rbc", (33, 17), dict(ra=3e4, dt=0.01, dealias=True, integrator="eu", beta=0.3, aspect=2.0), None),
+    ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True, integrator="rk3", beta=0.5), None),
+    ("zero", (40, 24), dict(ra=1e5, dt=0.01, dealias=True, integrator="eu", beta=0.7), False),
+]
+
+
+@pytest.mark.parametrize("case,shape,cfg,split", BETA_CASES,
+                         ids=[f"{c[0]}-{c[1][0]}x{c[1][1]}-{c[2]['integrator']}-{c[3]}" for c in BETA_CASES])
+def test_fused_beta_vs_oracle(NS, case, shape, cfg, split):
+    """beta != 1 (rbc2d.py:268-283, 390-391): beta-implicit ADI tables and pressure update, the explicit
+    diffusion through pass P2e and P3 / P3r; fused and per-field forms against the oracle."""
+    from pypde_gb300.navier.fused import FusedBatch
+    ns = NS(case=case, shape=shape, pr=1.0, tsave=None, **cfg)
+    ns.set_temperature_noise(9, 1e-2)
+    fb = FusedBatch([ns], split=split)
+    assert fb.beta and "P2e" in [p.name for p in fb.progs]
+    for _ in range(3):
+        fb.step_eager()
+    compare(ns, oracle_run(case, shape, cfg, 9, 1e-2, 3), 1e-8)
+
+
+def test_fused_beta_mixed_batch(NS):
+    """A batch mixing beta = 1 and beta != 1 instances: each against its own oracle run."""
+    from pypde_gb300.navier.fused import FusedBatch
+    specs = [((33, 33), 1e5, 1.0, 1), ((65, 33), 3e5, 0.5, 2), ((33, 17), 1e4, 0.25, 3)]
+    for split in (False, True):
+        solvers = []
+        for shape, ra, beta, seed in specs:
+            ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", beta=beta,
+                    tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers, split=split)
+        fb.capture(1)
+        for _ in range(3):
+            fb.step()
+        for ns, (shape, ra, beta, seed) in zip(solvers, specs):
+            ref = oracle_run("linear", shape, dict(ra=ra, dt=0.005, dealias=True, beta=beta), seed, 1e-3, 3)
+            compare(ns, ref, 1e-8)
+
+
+def test_fused_beta_golden(NS, golden):
+    """The reference's own run with beta = 0.5 (33 x 33, Ra 1e5, dt 0.01, seed 4 noise 1e-2): 5 fused steps."""
+    ns = NS(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", beta=0.5,
+            tsave=None)
+    ns.set_temperature_noise(4, 1e-2)
+    assert rel_err(ns.state()["T"], golden["rbc_beta33_T0"]) < 1e-10
+    f = ns.fused()
+    f.capture(1)
+    for _ in range(5):
+        f.step()
+    st = ns.state()
+    for name in ("T", "U", "V", "P", "pres"):
+        assert rel_err(st[name], golden[f"rbc_beta33_s5_{name}"]) < 1e-8, name
+
+
 RK3_CASES = [("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),
              ("rbc", (33, 17), dict(ra=1e5, dt=0.01, dealias=True)),
              ("zero", (33, 33), dict(ra=1e5, dt=0.01, dealias=True)),

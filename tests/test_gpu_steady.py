@@ -18,10 +18,11 @@ def torch():
     return torch
 
 
-def test_newton_krylov_fixed_point(torch):
+@pytest.mark.parametrize("beta", [1.0, 0.5])
+def test_newton_krylov_fixed_point(torch, beta):
     from oracle import rbc2d as orb
     from pypde_gb300.navier.rbc2d import NavierStokes
-    cfg = dict(case="linear", shape=(17, 17), ra=5e3, pr=1.0, dt=0.05, dealias=True, tsave=None)
+    cfg = dict(case="linear", shape=(17, 17), ra=5e3, pr=1.0, dt=0.05, dealias=True, tsave=None, beta=beta)
     ns = NavierStokes(integrator="eu", **cfg)
     ns.set_temperature_noise(1, 1e-1)
     for _ in range(100):
