@@ -106,6 +106,10 @@ enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_F
 /* op.k of DENSE: PGX_DENSE_MMA runs the contraction on the FP64 tensor cores (DMMA,
  * 8 x 8 x 4 tiles: rows x lines x columns) instead of one FMA chain per output. */
 #define PGX_DENSE_MMA 2
+/* Largest CTA: 1024 threads, 768 for programs with DCT ops (their kernel is compiled for up
+ * to 80 registers a thread; the kernel without the FFT code for 64). */
+#define PGX_MAX_THREADS 1024
+#define PGX_MAX_THREADS_FFT 768
 typedef struct pgx_op {
   int16_t code, a, b, arr, mat, len, par, k;
   double alpha;                    /* scalar; multiplied by par[par] when par >= 0 */
@@ -119,7 +123,8 @@ typedef struct pgx_program {
   int32_t nslots;                  /* slots used (<= PGX_MAX_SLOTS) */
   int32_t nops;
   int32_t fft_n;                   /* longest DCT length in the program, 0 if none */
-  int32_t nthreads;                /* CTA size (multiple of 32, <= 1024) */
+  int32_t nthreads;                /* CTA size (multiple of 32, <= PGX_MAX_THREADS; with DCT ops
+                                      <= PGX_MAX_THREADS_FFT) */
   pgx_op ops[PGX_MAX_OPS];
 } pgx_program;
 

@@ -68,7 +68,11 @@ static int check_program(const pgx_program* P) {
   if (!P) return PGX_E_ARG;
   if (P->axis < 0 || P->axis > 1 || P->tb < 1 || P->lcap < 1 || P->lcap > PGX_LMAX + 8) return PGX_E_ARG;
   if (P->nslots < 1 || P->nslots > PGX_MAX_SLOTS || P->nops < 0 || P->nops > PGX_MAX_OPS) return PGX_E_ARG;
-  if (P->nthreads < 32 || P->nthreads > 1024 || (P->nthreads & 31)) return PGX_E_ARG;
+  if (P->nthreads < 32 || P->nthreads > PGX_MAX_THREADS || (P->nthreads & 31)) return PGX_E_ARG;
+  bool has_dct = false;
+  for (int o = 0; o < P->nops; ++o) has_dct |= P->ops[o].code == PGX_OP_DCT;
+  // DCT ops need the FFT buffers (fft_n) and run in the kernel build for up to 768 threads
+  if (has_dct && (P->fft_n < 2 || P->nthreads > PGX_MAX_THREADS_FFT)) return PGX_E_ARG;
   if (P->lines_len < 0 || P->lines_len >= PGX_MAX_LEN) return PGX_E_ARG;
   if (P->fft_n > P->lcap) return PGX_E_ARG;
   for (int o = 0; o < P->nops; ++o) {
@@ -317,7 +321,7 @@ void pick_tile(pgx_program* P, int nlines, int maxlen, int nbuf, int fft_n) {
         op.k = (int16_t)(op.k | PGX_CHAIN_WARP);
     }
     int wt = 64 * tb;  // two chains (parities) per line, one warp each
-    P->nthreads = wt < 256 ? 256 : (wt > 1024 ? 1024 : wt);
+    P->nthreads = wt < 256 ? 256 : (wt > PGX_MAX_THREADS ? PGX_MAX_THREADS : wt);
   }
 }
 

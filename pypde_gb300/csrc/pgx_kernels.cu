@@ -30,6 +30,12 @@ __host__ __device__ inline int pgx_fft_stride(int n) {
   return ((n - 1) & 1) == 0 ? (n - 1) : 2 * (n - 1);
 }
 
+__host__ __device__ inline bool pgx_has_dct(const pgx_program& P) {
+  for (int o = 0; o < P.nops; ++o)
+    if (P.ops[o].code == PGX_OP_DCT) return true;
+  return false;
+}
+
 // Slots transformed together by one DCT op (op.b), the most of any DCT op of the program:
 // the FFT buffers hold that many slots' line pairs.
 __host__ __device__ inline int pgx_fft_slots(const pgx_program& P) {
@@ -725,6 +731,13 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+// p + w q and 2 p - z, each component one or two fused multiply-adds
+__device__ __forceinline__ double2 cmadd(double2 p, double2 w, double2 q) {
+  return make_double2(fma(w.x, q.x, fma(-w.y, q.y, p.x)), fma(w.x, q.y, fma(w.y, q.x, p.y)));
+}
+__device__ __forceinline__ double2 ctwice_minus(double2 p, double2 z) {
+  return make_double2(fma(2.0, p.x, -z.x), fma(2.0, p.y, -z.y));
+}
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 
 // Diagonal scalings around the raw DCT-I matrix C (y = post * C (pre * x)), per mode:
@@ -802,11 +815,30 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
         v[r] = src[pr * c.fft_stride + m];
       }
     }
+    double2 o[R];
+    if (R != 3 && Ns > 1 && !FIRST && !LAST) {
+      // Twiddled radix-2 / radix-4 butterflies as fused multiply-adds (w2 = w1^2, w3 = w1 w2):
+      //   a = v0 + w2 v2, b = 2 v0 - a, c = v1 + w2 v3, d = 2 v1 - c,
+      //   o0 = a + w1 c, o2 = 2a - o0, o1 = b + (-i w1) d, o3 = 2b - o1
+      // (24 FP64 instructions against 28 for three complex products and eight sums).
+      const double2 w1 = __ldg(tw + k * step);
+      if (R == 2) {
+        o[0] = cmadd(v[0], w1, v[1]);
+        o[1] = ctwice_minus(v[0], o[0]);
+      } else {
+        const double2 w2 = __ldg(tw + 2 * k * step);
+        const double2 a = cmadd(v[0], w2, v[2]), b = ctwice_minus(v[0], a);
+        const double2 cc = cmadd(v[1], w2, v[3]), d = ctwice_minus(v[1], cc);
+        o[0] = cmadd(a, w1, cc);
+        o[2] = ctwice_minus(a, o[0]);
+        o[1] = cmadd(b, make_double2(w1.y, -w1.x), d);
+        o[3] = ctwice_minus(b, o[1]);
+      }
+    } else {
     if (k != 0) {
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + k * r * step));
     }
-    double2 o[R];
     if (R == 2) {
       o[0] = cadd(v[0], v[1]);
       o[1] = csub(v[0], v[1]);
@@ -825,6 +857,7 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
       o[0] = cadd(v[0], t1);
       o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));  // t2 - i h t3
       o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));  // t2 + i h t3
+    }
     }
     const int base = (j - k) * R + k;
 #pragma unroll
@@ -885,6 +918,11 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   const int npairs = (c.tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
+  if (N > c.fft_stride) {  // FFT buffers sized for a shorter length: refuse loudly
+    for (int sl = 0; sl < ns; ++sl)
+      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+    return;
+  }
   // fold
   for (int idx = c.tid; idx < nall * N; idx += c.nthreads) {
     const int P = idx / N, j = idx - P * N;
@@ -910,19 +948,20 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   // y_1: one warp per line (line lt = sl * tb + t)
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+    const bool alt = op.k == PGX_DCT_BWD || op.k == PGX_DCT_FWD_T;
+    const double ps = ds.has_pre ? (alt ? -ds.pre(1, N) : ds.pre(1, N)) : 1.0;
     for (int lt = warp; lt < ns * c.tb; lt += nw) {
       const int sl = lt / c.tb, t = lt - sl * c.tb;
       const double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
+      // the interior pre-scale is ps (-1)^j (alt) or ps: the sign is fixed per lane (j = 1 + lane
+      // mod 32), the magnitude applied once
       double acc = 0.0;
-      for (int j = 1 + lane; j < H; j += 32) {
-        double d = xl[j] - xl[N - j];
-        if (ds.has_pre) d *= ds.pre(j, N);
-        acc = fma(__ldg(&tw[j].x), d, acc);
-      }
+      for (int j = 1 + lane; j < H; j += 32) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
+      if (alt && ((1 + lane) & 1)) acc = -acc;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       const double d0 = (xl[0] - xl[N]) * (ds.has_pre ? ds.pre(0, N) : 1.0);
-      if (lane == 0) c.ybuf[lt] = fma(2.0, acc, d0);
+      if (lane == 0) c.ybuf[lt] = fma(2.0 * ps, acc, d0);
     }
   }
   __syncthreads();
@@ -982,9 +1021,16 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
         if (lane >= o) incl += v;
       }
       double pre = incl - run;  // exclusive prefix of this lane's chunk
-      for (int m = m0; m < m1; ++m) {
-        pre += xl[2 * m + 1];
-        xl[2 * m + 1] = pre * osc;
+      if (ds.has_post) {
+        for (int m = m0; m < m1; ++m) {
+          pre += xl[2 * m + 1];
+          xl[2 * m + 1] = pre * osc;
+        }
+      } else {
+        for (int m = m0; m < m1; ++m) {
+          pre += xl[2 * m + 1];
+          xl[2 * m + 1] = pre;
+        }
       }
     }
   }
@@ -1059,7 +1105,7 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
 }
 
 // ------------------------------------------------------------------ driver
-template <bool BATCHED>
+template <bool BATCHED, bool FFT>
 __device__ void run_program(const pgx_program& P, const pgx_instance& I, int tile) {
   extern __shared__ __align__(16) double smem_dyn[];
   Ctx c;
@@ -1102,7 +1148,9 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
       case PGX_OP_STENCIL_T: op_stencil_t(c, op, I); break;
       case PGX_OP_TDMA2: op_tdma2(c, op, I); break;
       case PGX_OP_DIFF: op_diff(c, op); break;
-      case PGX_OP_DCT: op_dct(c, op, I); break;
+      case PGX_OP_DCT:
+        if (FFT) op_dct(c, op, I);  // programs with DCT ops run the FFT kernels only
+        break;
       case PGX_OP_BANDED: op_banded(c, op, I); break;
       case PGX_OP_DENSE: op_dense(c, op, I); break;
       case PGX_OP_FDMA: op_fdma(c, op, I, false); break;
@@ -1119,13 +1167,9 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   }
 }
 
-// Up to 1024 threads a block (one warp per chain line): at most 64 registers a thread.
-__global__ void __launch_bounds__(1024) line_program_single(const __grid_constant__ pgx_program P, const __grid_constant__ pgx_instance I) {
-  run_program<false>(P, I, blockIdx.x);
-}
-
-__global__ void __launch_bounds__(1024) line_program_batched(const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts,
-                                     const int32_t* __restrict__ work) {
+template <bool FFT>
+__device__ __forceinline__ void run_batched(const pgx_program& P, const pgx_instance* __restrict__ insts,
+                                            const int32_t* __restrict__ work) {
   extern __shared__ __align__(16) double smem_dyn[];
   pgx_instance* sI = reinterpret_cast<pgx_instance*>(smem_dyn);
   const int inst = work[2 * blockIdx.x], tile = work[2 * blockIdx.x + 1];
@@ -1134,7 +1178,30 @@ __global__ void __launch_bounds__(1024) line_program_batched(const __grid_consta
   double* dst = reinterpret_cast<double*>(sI);
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
   __syncthreads();
-  run_program<true>(P, *sI, tile);
+  run_program<true, FFT>(P, *sI, tile);
+}
+
+// Two builds of the interpreter: with the FFT code (programs with DCT ops; up to 768 threads,
+// 80 registers a thread without spills) and without it (up to 1024 threads, 64 registers).
+__global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_single(const __grid_constant__ pgx_program P,
+                                                                       const __grid_constant__ pgx_instance I) {
+  run_program<false, false>(P, I, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_single_fft(const __grid_constant__ pgx_program P,
+                                                                               const __grid_constant__ pgx_instance I) {
+  run_program<false, true>(P, I, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_batched(const __grid_constant__ pgx_program P,
+                                                                        const pgx_instance* __restrict__ insts,
+                                                                        const int32_t* __restrict__ work) {
+  run_batched<false>(P, insts, work);
+}
+
+__global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_batched_fft(
+    const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts, const int32_t* __restrict__ work) {
+  run_batched<true>(P, insts, work);
 }
 
 }  // namespace pgx
@@ -1158,7 +1225,7 @@ namespace pgx {
 // could invalidate by setting a lower value.
 static int raise_smem_cap(const void* fn, int which) {
   static std::mutex mu;
-  static bool done[2][64] = {};
+  static bool done[4][64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
@@ -1176,22 +1243,28 @@ static int raise_smem_cap(const void* fn, int which) {
 
 int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles) {
   int64_t smem = pgx_program_smem(P);
+  const bool fft = pgx_has_dct(*P);
   if (smem > 48 * 1024) {
-    int e = raise_smem_cap((const void*)line_program_single, 0);
+    int e = fft ? raise_smem_cap((const void*)line_program_single_fft, 2)
+                : raise_smem_cap((const void*)line_program_single, 0);
     if (e) return e;
   }
-  line_program_single<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
+  if (fft) line_program_single_fft<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
+  else line_program_single<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
   return (int)cudaGetLastError();
 }
 
 int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
                    cudaStream_t s) {
   int64_t smem = pgx_program_smem(P) + ((sizeof(pgx_instance) + 15) / 16) * 16;
+  const bool fft = pgx_has_dct(*P);
   if (smem > 48 * 1024) {
-    int e = raise_smem_cap((const void*)line_program_batched, 1);
+    int e = fft ? raise_smem_cap((const void*)line_program_batched_fft, 3)
+                : raise_smem_cap((const void*)line_program_batched, 1);
     if (e) return e;
   }
-  line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  if (fft) line_program_batched_fft<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  else line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
   return (int)cudaGetLastError();
 }
 }  // namespace pgx

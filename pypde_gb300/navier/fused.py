@@ -888,9 +888,16 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     nt = max(256, 32 * -(-width * tb // 32))
     # few chains in the whole launch: one warp per chain (scanned) instead of one thread
     wc = chains and width * lines_total < 152 * 64
+    ntmax = _max_threads(prog, fft_n, False)
     if wc:
-        nt = max(256, min(1024, 32 * width * tb))
-    return tb, min(nt, 1024), bool(wc), sd, False
+        nt = max(256, min(ntmax, 32 * width * tb))
+    return tb, min(nt, ntmax), bool(wc), sd, False
+
+
+def _max_threads(prog, fft_n, dm):
+    """CTA size limit of a launch: programs that keep DCT ops run the FFT build of the kernel."""
+    fft = fft_n > 1 and not dm and any(o.code == _lib.OP["DCT"] for o in prog.ops)
+    return _lib.MAX_THREADS_FFT if fft else _lib.MAX_THREADS
 
 
 def _candidates(prog, lines_total, lcap, fft_n, max_lines):
@@ -912,6 +919,7 @@ def _has_dense(prog, fft_n):
 
 
 def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, dm):
+    ntmax = _max_threads(prog, fft_n, dm)
     nbuf = prog.nslots + 1
     per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
     width = 1
@@ -935,12 +943,12 @@ def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, dm):
             continue
         for nt in (256, 512):
             nt = max(nt, 32 * -(-width * tb // 32))
-            if nt <= 1024 and (tb, nt, False, sd, dm) not in out:
+            if nt <= ntmax and (tb, nt, False, sd, dm) not in out:
                 out.append((tb, nt, False, sd, dm))
-        if chains:  # warp-per-chain variants: a warp for each of the CTA's chains, up to 1024 threads
-            for nt in (256, min(1024, 32 * width * tb)):
+        if chains:  # warp-per-chain variants: a warp for each of the CTA's chains, up to ntmax
+            for nt in (256, min(ntmax, 32 * width * tb)):
                 nt = max(nt, 256)
-                if nt <= 1024 and (tb, nt, True, sd, dm) not in out:
+                if nt <= ntmax and (tb, nt, True, sd, dm) not in out:
                     out.append((tb, nt, True, sd, dm))
     return out
 
