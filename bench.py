@@ -272,7 +272,14 @@ def run_gpu(args, rank, world):
     if args.save_tiles:
         with open(args.save_tiles, "w") as f:
             json.dump({"forward": fb.tiles()}, f)
-    fb.capture(1)
+    if args.graph_groups:
+        fb.capture(1, groups=args.graph_groups)
+        group_times = None
+    elif args.no_tune:
+        fb.capture(1)
+        group_times = None
+    else:  # instance groups as parallel branches of the step's graph: tuned like the tiles
+        group_times = {str(k): round(v, 4) for k, v in fb.tune_groups().items()}
     state_bytes = fb.state_arena.numel() * 8
     work_bytes = fb.scratch_bytes()
 
@@ -299,14 +306,15 @@ def run_gpu(args, rank, world):
     value = aggregate_value(n_inst, world, args.steps, total_ms)
     finite = int(sum(bool(torch.isfinite(I.arrays["TG"]).all()) for I in fb.insts))
 
-    # e2e: public API, state in pinned host memory, H2D before and D2H after every step
+    # e2e: public API (FusedBatch.step_host), state in pinned host memory, copied in before and out
+    # after every step; instance groups on their own streams overlap one group's copies with
+    # another's passes
     host = torch.empty(fb.state_arena.numel(), dtype=torch.float64, pin_memory=True)
     host.copy_(fb.state_arena)
+    groups = fb.host_pipeline(args.e2e_groups)
 
     def e2e_step():
-        fb.state_arena.copy_(host, non_blocking=True)
-        fb.step()
-        host.copy_(fb.state_arena, non_blocking=True)
+        fb.step_host(host)
 
     for _ in range(2):
         e2e_step()
@@ -316,7 +324,7 @@ def run_gpu(args, rank, world):
     if world > 1:
         e2e_total = max_over_ranks(e2e_total)
     e2e = {"value": n_inst * world * args.steps / (e2e_total / 1e3), "unit": "instance-steps/s",
-           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes}
+           "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes, "stream_groups": groups}
 
     if rank != 0:
         return None
@@ -392,18 +400,20 @@ def run_gpu(args, rank, world):
         "data": "synthetic: seeded U(-1,1) temperature noise on the conductive profile (seeds 100+i)",
         "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=n_inst), "instances_per_gpu": n_inst,
                    "sizes": sorted({s[0] for s in specs}),
-                   "form": "batched, CUDA-graph replay of %d fused passes%s" % (
-                       len(fb.progs), " (per-field convection passes)" if fb.split else ""),
+                   "form": "batched, CUDA-graph replay of %d fused passes%s, instances in %d parallel graph "
+                           "branches" % (len(fb.progs), " (per-field convection passes)" if fb.split else "",
+                                         fb.graph_groups),
                    "l2": "no flush: the working set (state %.1f MB + scratch %.1f MB) exceeds the 129 MB L2"
                          % (state_bytes / 1e6, work_bytes / 1e6), "parallelism": "instance-parallel"},
         "e2e": e2e,
-        "gpu_launches": fb.launches_per_step * args.steps,
+        "gpu_launches": fb.graph_launches * args.steps,
         "roofline": roofline,
         "step_fp64": step_fp64,
         "passes": passes,
         "plain": plain,
         "eager": eager,
         "autotuned_tiles": tuned,
+        "graph_groups": {"groups": fb.graph_groups, "tuned_ms_per_step": group_times},
         "finite_instances": finite,
         "host_wall_s": round(wall, 3),
     }
@@ -661,6 +671,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
+    ap.add_argument("--graph-groups", type=int, default=0,
+                    help="instance groups as parallel branches of the step's graph (0: tuned)")
+    ap.add_argument("--e2e-groups", type=int, default=4,
+                    help="instance groups of the end-to-end step, each on its own stream")
     ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],
                     help="per-field convection passes (auto: for batches of up to 4 instances)")
     ap.add_argument("--save-tiles", default=None)

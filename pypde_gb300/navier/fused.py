@@ -1071,14 +1071,16 @@ class FusedBatch:
         return {"name": name or prog.name, "P": P, "d_insts": d_insts, "d_work": d_work, "nwork": len(work),
                 "key": key, "members": members, "prog": prog, "wc": bool(wc), "sd": bool(sd), "dm": bool(dm)}
 
-    def _pass_launches(self, prog, tiles=None, stage=0):
+    def _pass_launches(self, prog, tiles=None, stage=0, key_tiles=None):
         d_insts = self._d_insts(prog, stage)
         name = prog.name if stage == 0 else "%s@%d" % (prog.name, stage)
         out = []
         for gi, (key, members) in enumerate(self._groups(prog)):
             lines = [self.insts[k].lines(prog) for k in members]
             tag = "%s#%d" % (name, gi)
-            if tiles and tag in tiles:
+            if key_tiles and (name, key) in key_tiles:
+                tb, nt, wc, sd, dm = key_tiles[(name, key)]
+            elif tiles and tag in tiles:
                 tb, nt, wc, sd, dm = (tuple(tiles[tag][:5]) + (False,) * 3)[:5]
             else:
                 tb, nt, wc, sd, dm = _pick(prog, sum(lines) * len(prog.variants), key[0], key[1], max(lines))
@@ -1154,8 +1156,10 @@ class FusedBatch:
         for i in range(len(self.launches)):
             self.run_pass(i)
 
-    def capture(self, nsteps=1):
-        """Record ``nsteps`` fused steps in a CUDA graph; ``step()`` then replays it."""
+    def capture(self, nsteps=1, groups=1):
+        """Record ``nsteps`` fused steps in a CUDA graph; ``step()`` then replays it.  ``groups`` > 1:
+        the instances in that many groups (``_split_groups``), each group's launches a parallel
+        branch of the graph, so one group's next pass starts while another's drains."""
         # the passes update the state in place: keep a copy, warm up once outside the
         # capture (kernel attributes, lazy tables), restore, then record
         saved = [{k: I.arrays[k].clone() for k in ("UG", "VG", "TG", "PG", "PRES")} for I in self.insts]
@@ -1164,15 +1168,30 @@ class FusedBatch:
         for I, s in zip(self.insts, saved):
             for k, v in s.items():
                 I.arrays[k].copy_(v)
+        branches = []
+        if groups > 1:
+            branches = [(self._subset(idx), torch.cuda.Stream()) for idx, _, _ in self._split_groups(groups)]
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
+            cur = torch.cuda.current_stream()
             for _ in range(nsteps):
-                self.step_eager()
+                if len(branches) > 1:
+                    for sub, st in branches:
+                        st.wait_stream(cur)
+                        with torch.cuda.stream(st):
+                            sub.step_eager()
+                    for _, st in branches:
+                        cur.wait_stream(st)
+                else:
+                    self.step_eager()
         torch.cuda.synchronize()
         for I, s in zip(self.insts, saved):
             for k, v in s.items():
                 I.arrays[k].copy_(v)
         self.graph, self.graph_steps = g, nsteps
+        self.graph_groups = max(1, len(branches))
+        self.graph_launches = sum(sub.launches_per_step for sub, _ in branches) if len(branches) > 1 \
+            else self.launches_per_step
 
     def step(self):
         """One fused step (graph replay when captured with nsteps == 1)."""
@@ -1184,6 +1203,84 @@ class FusedBatch:
     @property
     def launches_per_step(self):
         return sum(len(g) for g in self.launches)
+
+    # ------------------------------------------------- host-resident state
+    def _subset(self, idx):
+        """Launch set of the instances ``idx`` (same state, scratch and tables), each launch with
+        the tile this batch uses for the same pass and size class."""
+        key_tiles = {(L["name"], L["key"]): (L["P"].tb, L["P"].nthreads, L["wc"], L["sd"], L["dm"])
+                     for group in self.launches for L in group}
+        sub = FusedBatch.__new__(FusedBatch)
+        sub.solvers, sub.insts = [self.solvers[i] for i in idx], [self.insts[i] for i in idx]
+        sub.fft, sub.nstage, sub.tkind, sub.split, sub.beta = self.fft, self.nstage, self.tkind, self.split, self.beta
+        sub.progs, sub.state_arena, sub.graph = self.progs, None, None
+        sub.launches = [sub._pass_launches(p, None, st, key_tiles) for st in range(sub.nstage) for p in sub.progs]
+        return sub
+
+    def tune_groups(self, candidates=(1, 2, 4, 8, 16), reps=5):
+        """Capture the step with each number of instance groups (parallel graph branches), time
+        ``reps`` replays of each and keep the fastest; the state is restored after every trial.
+        Returns {groups: ms per step}."""
+        saved = self.state_arena.clone()
+        times = {}
+        for G in candidates:
+            if G > len(self.insts):
+                continue
+            self.capture(1, groups=G)
+            self.step()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                self.step()
+            b.record()
+            torch.cuda.synchronize()
+            times[G] = a.elapsed_time(b) / reps
+            self.state_arena.copy_(saved)
+        best = min(times, key=times.get)
+        self.capture(1, groups=best)
+        torch.cuda.synchronize()
+        return times
+
+    def _split_groups(self, groups):
+        """[(instance indices, first, end offset in state_arena)]: up to ``groups`` contiguous groups
+        of instances of about equal state size."""
+        base = self.state_arena.data_ptr()
+        starts = [(I.arrays["UG"].data_ptr() - base) // 8 for I in self.insts] + [self.state_arena.numel()]
+        cum = np.cumsum(np.diff(starts))
+        cuts = [0] + [int(np.searchsorted(cum, cum[-1] * g / groups)) + 1 for g in range(1, groups)] + [len(cum)]
+        cuts = sorted(set(min(max(c, 0), len(cum)) for c in cuts))
+        return [(range(a, b), starts[a], starts[b]) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+
+    def host_pipeline(self, groups=2):
+        """Prepare ``step_host``: the instances in ``groups`` contiguous groups of about equal state
+        size, each with its own launch set, CUDA graph and stream."""
+        self._pipe = []
+        for idx, o0, o1 in self._split_groups(groups):
+            sub = self._subset(idx)
+            sub.capture(1)
+            self._pipe.append((sub, o0, o1, torch.cuda.Stream()))
+        self._pipe_fresh = True
+        return len(self._pipe)
+
+    def step_host(self, host):
+        """One step of every instance with the state in host memory: ``host`` (pinned, the layout of
+        ``state_arena``) is copied in, stepped and copied back.  The instance groups of
+        ``host_pipeline`` run on their own streams, so one group's copies overlap another's
+        passes and the next step's upload of a group follows its own download; the current
+        stream waits for all groups before the call returns (asynchronously)."""
+        if getattr(self, "_pipe", None) is None:
+            self.host_pipeline()
+        main = torch.cuda.current_stream()
+        for sub, o0, o1, st in self._pipe:
+            if self._pipe_fresh:
+                st.wait_stream(main)
+            with torch.cuda.stream(st):
+                self.state_arena[o0:o1].copy_(host[o0:o1], non_blocking=True)
+                sub.step()
+                host[o0:o1].copy_(self.state_arena[o0:o1], non_blocking=True)
+        self._pipe_fresh = False
+        for *_, st in self._pipe:
+            main.wait_stream(st)
 
     def single(self, i):
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""

@@ -219,6 +219,38 @@ def test_tensor_core_contractions_match(NS):
         compare(ns, ref, 1e-8)
 
 
+def test_step_host_pipeline_matches_step(NS):
+    """FusedBatch.step_host (state in pinned host memory, instance groups on their own streams) and
+    a step graph with the instance groups as parallel branches give exactly the one-stream graph step."""
+    import torch
+    from pypde_gb300.navier.fused import FusedBatch
+    specs = [((33, 33), 1e4, 1), ((65, 33), 1e5, 2), ((33, 65), 3e5, 3), ((17, 17), 1e4, 4), ((65, 65), 1e6, 5)]
+    runs = []
+    for host_mode in (False, True, "branches"):
+        solvers = []
+        for shape, ra, seed in specs:
+            ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=True, integrator="eu", tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers)
+        fb.capture(1, groups=3 if host_mode == "branches" else 1)
+        if host_mode is True:
+            assert fb.host_pipeline(3) >= 2
+            host = torch.empty(fb.state_arena.numel(), dtype=torch.float64, pin_memory=True)
+            host.copy_(fb.state_arena)
+            for _ in range(4):
+                fb.step_host(host)
+            torch.cuda.synchronize()
+            runs.append(host.clone())
+        else:
+            for _ in range(4):
+                fb.step()
+            torch.cuda.synchronize()
+            runs.append(fb.state_arena.cpu())
+    assert fb.graph_groups >= 2
+    assert torch.equal(runs[0], runs[1]) and torch.equal(runs[0], runs[2])
+
+
 BETA_CASES = [
     ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True, integrator="eu", beta=0.5), None),
     ("linear", (33, 33), dict(ra=1e5, dt=0.01, dealias=True, integrator="eu", beta=0.5), False),
