@@ -273,7 +273,7 @@ def run_gpu(args, rank, world):
         with open(args.save_tiles, "w") as f:
             json.dump({"forward": fb.tiles()}, f)
     if args.graph_groups:
-        fb.capture(1, groups=args.graph_groups)
+        fb.capture(1, groups="shape" if args.graph_groups < 0 else args.graph_groups)
         group_times = None
     elif args.no_tune:
         fb.capture(1)
@@ -672,7 +672,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
     ap.add_argument("--graph-groups", type=int, default=0,
-                    help="instance groups as parallel branches of the step's graph (0: tuned)")
+                    help="instance groups as parallel branches of the step's graph (0: tuned, -1: one "
+                         "per instance shape)")
     ap.add_argument("--e2e-groups", type=int, default=4,
                     help="instance groups of the end-to-end step, each on its own stream")
     ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],

@@ -1169,7 +1169,12 @@ class FusedBatch:
             for k, v in s.items():
                 I.arrays[k].copy_(v)
         branches = []
-        if groups > 1:
+        if groups == "shape":  # one branch per instance shape: every launch of a branch is one size class
+            shapes = {}
+            for k, I in enumerate(self.insts):
+                shapes.setdefault((I.N, I.M), []).append(k)
+            branches = [(self._subset(idx), torch.cuda.Stream()) for idx in shapes.values()]
+        elif groups > 1:
             branches = [(self._subset(idx), torch.cuda.Stream()) for idx, _, _ in self._split_groups(groups)]
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
@@ -1189,6 +1194,8 @@ class FusedBatch:
             for k, v in s.items():
                 I.arrays[k].copy_(v)
         self.graph, self.graph_steps = g, nsteps
+        # the graph reads the branches' instance descriptors and work lists: they live as long as it
+        self.graph_branches = branches
         self.graph_groups = max(1, len(branches))
         self.graph_launches = sum(sub.launches_per_step for sub, _ in branches) if len(branches) > 1 \
             else self.launches_per_step
@@ -1217,14 +1224,14 @@ class FusedBatch:
         sub.launches = [sub._pass_launches(p, None, st, key_tiles) for st in range(sub.nstage) for p in sub.progs]
         return sub
 
-    def tune_groups(self, candidates=(1, 2, 4, 8, 16), reps=5):
+    def tune_groups(self, candidates=(1, 2, 4, 8, 16, "shape"), reps=5):
         """Capture the step with each number of instance groups (parallel graph branches), time
-        ``reps`` replays of each and keep the fastest; the state is restored after every trial.
-        Returns {groups: ms per step}."""
+        ``reps`` replays of each and keep the fastest ("shape": one branch per instance shape); the
+        state is restored after every trial.  Returns {groups: ms per step}."""
         saved = self.state_arena.clone()
         times = {}
         for G in candidates:
-            if G > len(self.insts):
+            if G != "shape" and G > len(self.insts):
                 continue
             self.capture(1, groups=G)
             self.step()
@@ -1257,7 +1264,7 @@ class FusedBatch:
         self._pipe = []
         for idx, o0, o1 in self._split_groups(groups):
             sub = self._subset(idx)
-            sub.capture(1)
+            sub.capture(1, groups="shape")
             self._pipe.append((sub, o0, o1, torch.cuda.Stream()))
         self._pipe_fresh = True
         return len(self._pipe)
