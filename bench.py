@@ -432,7 +432,7 @@ def run_adjoint(args, stream):
     reverse-mode passes; central differences (h = 1e-6) on 20 random unit directions; descent."""
     import torch
     from pypde_gb300.navier.adjoint import descend, random_directions
-    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient, HorizonGradientGroups
     from pypde_gb300.navier.rbc2d import NavierStokes
     H, every, shape = args.adjoint_horizon, 20, (129, 129)
     ns = NavierStokes(case="linear", shape=shape, ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu",
@@ -495,20 +495,16 @@ def run_adjoint(args, stream):
                                tsave=None)
             nsi.set_temperature_noise(3 + i, 1e-2)
             solvers.append(nsi)
-        fab = FusedAdjoint(solvers)
-        if not args.no_tune:
-            fab.autotune(reps=2)
-            fab.autotune_adjoint(reps=2)
-        hgb = HorizonGradient(fab, H, every)
-        Xb = fab.state_arena.clone()
+        hgs = HorizonGradientGroups(solvers, H, every, groups=args.adjoint_groups, tune=not args.no_tune)
+        Xs = hgs.states()
         for _ in range(2):
-            hgb.value_and_grad(Xb)
+            hgs.value_and_grad(Xs)
         torch.cuda.synchronize()
-        ms_b, (Jb, gb) = timed(lambda: hgb.value_and_grad(Xb), 2)
-        batched = {"instances": args.adjoint_batch, "ms_per_batch_grad": round(ms_b, 3),
+        ms_b, outs = timed(lambda: hgs.value_and_grad(Xs), 2)
+        batched = {"instances": args.adjoint_batch, "groups": len(hgs.parts), "ms_per_batch_grad": round(ms_b, 3),
                    "grads_per_s": round(args.adjoint_batch * 1e3 / ms_b, 3),
-                   "finite": bool(torch.isfinite(gb).all())}
-        del hgb, fab, solvers
+                   "finite": all(bool(torch.isfinite(g).all()) for _, g in outs)}
+        del hgs, outs, solvers
         torch.cuda.empty_cache()
     # steady-state search: descent iterations, one gradient evaluation each
     t0 = time.perf_counter()
@@ -671,6 +667,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
+    ap.add_argument("--adjoint-groups", type=int, default=1,
+                    help="instance groups of the batched gradient, each on its own stream (measured on the "
+                         "32-instance batch: 1 group 22.5, 4 groups 20.5, 8 groups 17.0 gradients/s)")
     ap.add_argument("--graph-groups", type=int, default=0,
                     help="instance groups as parallel branches of the step's graph (0: tuned, -1: one "
                          "per instance shape)")

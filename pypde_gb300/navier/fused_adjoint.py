@@ -644,6 +644,43 @@ class HorizonGradient:
 
 
 
+class HorizonGradientGroups:
+    """Horizon gradients of many instances as ``groups`` independent FusedAdjoint / HorizonGradient
+    pairs (contiguous instance groups), each replayed on its own stream: the groups' sequential
+    sweeps overlap, filling the SMs that one group's small launches leave idle."""
+
+    def __init__(self, solvers, nsteps, every=20, groups=4, tune=True):
+        bounds = [round(len(solvers) * g / groups) for g in range(groups + 1)]
+        self.parts = []
+        for a, b in zip(bounds[:-1], bounds[1:]):
+            if b <= a:
+                continue
+            fa = FusedAdjoint(solvers[a:b])
+            if tune:
+                fa.autotune(reps=2)
+                fa.autotune_adjoint(reps=2)
+            self.parts.append((fa, HorizonGradient(fa, nsteps, every), torch.cuda.Stream()))
+
+    def states(self):
+        """Copies of every group's state arena (the layout value_and_grad takes)."""
+        return [fa.state_arena.clone() for fa, _, _ in self.parts]
+
+    def value_and_grad(self, Xs):
+        """[(J, dJ/dX)] per group for the group states ``Xs``; the current stream waits for all."""
+        main = torch.cuda.current_stream()
+        out = []
+        for (_, hg, st), X in zip(self.parts, Xs):
+            st.wait_stream(main)
+            with torch.cuda.stream(st):
+                J, g = hg.value_and_grad(X)
+            J.record_stream(main)
+            g.record_stream(main)
+            out.append((J, g))
+        for _, _, st in self.parts:
+            main.wait_stream(st)
+        return out
+
+
 class FusedHorizon(torch.autograd.Function):
     """Y = Phi^H(X) on the fused passes, differentiable: backward runs the fused reverse-mode
     passes over the checkpointed horizon.  X and Y are whole-batch state arenas (``fa.views``

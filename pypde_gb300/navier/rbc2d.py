@@ -285,6 +285,27 @@ class NavierStokes(NavierStokesBase, NavierStokesSteadyState, Integrator):
         for _ in range(nsteps):
             f.step()
 
+    def iterate(self, maxtime, callback=True, fused=None):
+        """The time loop of integrator.py:14-32 (steps, time, save / callback every ``tsave``).  The
+        steps are replays of the fused step's CUDA graph (``fused=None``: whenever autograd is not
+        recording through the state), else ``update()``; both give the reference's step."""
+        if fused is None:
+            fused = not (torch.is_grad_enabled() and any(getattr(self, k).vhat.requires_grad
+                                                         for k in ("T", "U", "V", "P", "pres")))
+        if not fused:
+            return Integrator.iterate(self, maxtime, callback)
+        f = self.fused()
+        if f.graph is None:
+            f.capture(1)
+        eps = 1e-3 * self.dt
+        while (self.time + eps) < maxtime:
+            f.step()
+            self.update_time()
+            if self.tsave is not None and (self.time + eps) % self.tsave < self.dt * 0.5:
+                self.save()
+                if callback:
+                    self.callback()
+
     # -- state as host arrays
     def state(self):
         return {k: to_host(getattr(self, k).vhat) for k in ("T", "U", "V", "P", "pres")}

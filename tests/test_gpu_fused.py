@@ -347,3 +347,23 @@ def test_fused_rk3_golden(NS, golden):
     st = ns.state()
     for name in ("T", "U", "V", "P", "pres"):
         assert rel_err(st[name], golden[f"rbc_rk3_33_s5_{name}"]) < 1e-8, name
+
+
+def test_iterate_fused_matches_update_loop(NS):
+    """NavierStokes.iterate (integrator.py:14-32) on the fused graph step gives the update() loop's state,
+    time and callback schedule."""
+    out = []
+    for fused in (False, True):
+        ns = NS(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", tsave=None)
+        ns.set_temperature_noise(3, 1e-2)
+        calls = []
+        ns.save = lambda: None
+        ns.callback = lambda: calls.append(round(ns.time, 8))
+        ns.tsave = 0.05
+        ns.iterate(0.2, fused=fused)
+        assert (ns._fused is not None) == fused
+        out.append((ns.state(), ns.time, calls))
+    (a, ta, ca), (b, tb, cb) = out
+    assert abs(ta - tb) < 1e-12 and ca == cb and len(ca) == 4
+    for k in a:
+        assert rel_err(b[k], a[k]) < 1e-11, k

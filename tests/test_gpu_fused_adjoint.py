@@ -230,3 +230,31 @@ def test_fused_horizon_autograd_function(torch):
         assert rel_err(gv[k].cpu().numpy(), r.cpu().numpy()) < 1e-9, k
     J2, g2 = hg.value_and_grad(Xa.detach())   # (U, V, T entries only; FusedHorizon also gives d/d pres)
     assert float((g2 - Xa.grad * mask).abs().max() / g2.abs().max()) < 1e-12
+
+
+def test_horizon_gradient_groups_match_one_batch(torch):
+    """HorizonGradientGroups (instance groups replayed on their own streams) gives each instance the
+    gradient of the one-batch HorizonGradient."""
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient, HorizonGradientGroups
+    H, every = 6, 3
+    mk = lambda s: _ns("linear", (33, 17), ra=2e4 * (1 + s), dt=0.005)  # noqa: E731
+    solvers = [mk(s) for s in range(5)]
+    for s, ns in enumerate(solvers):
+        _random_state(torch, ns, 30 + s)
+    fa = FusedAdjoint([mk(s) for s in range(5)])
+    for v, ns in zip(fa.views(fa.state_arena), solvers):
+        for k, f in (("TG", "T"), ("UG", "U"), ("VG", "V")):
+            v[k].copy_(getattr(ns, f).vhat)
+    J1, g1 = HorizonGradient(fa, H, every).value_and_grad(fa.state_arena.clone())
+    hgs = HorizonGradientGroups(solvers, H, every, groups=3, tune=False)
+    assert len(hgs.parts) == 3
+    outs = hgs.value_and_grad(hgs.states())
+    torch.cuda.synchronize()
+    i = 0
+    for (fa_g, _, _), (J, g) in zip(hgs.parts, outs):
+        for k in range(len(fa_g.insts)):
+            assert abs(float(J[k]) - float(J1[i])) <= 1e-12 * abs(float(J1[i]))
+            ref = fa.views(g1)[i]
+            for key, v in fa_g.views(g)[k].items():
+                assert rel_err(v.cpu().numpy(), ref[key].cpu().numpy()) < 1e-11, (i, key)
+            i += 1
