@@ -89,3 +89,25 @@ def test_fused_programs_fit_the_abi(tkind, fft):
             assert o.len < _lib.MAX_LEN and o.par < _lib.MAX_PAR
         # every array stored is either state or scratch; every loaded array is defined
         assert p.axis in (0, 1)
+
+
+def test_program_checks_reject_malformed_dct_ops():
+    """pgx_run refuses, before any launch, programs whose DCT ops could not run: no FFT buffers
+    (fft_n < 2), more slots than the program has, or a CTA above the FFT build's 768 threads."""
+    from pypde_gb300 import _lib
+    L = _lib.lib()
+
+    def prog(fft_n=9, nthreads=256, b=1, nslots=1):
+        P = _lib.PgxProgram()
+        P.axis, P.lines_len, P.tb, P.lcap, P.nslots, P.fft_n, P.nthreads = 0, 1, 2, 11, nslots, fft_n, nthreads
+        ops = [_lib.op("LOAD", a=0, arr=0, len=0), _lib.op("DCT", a=0, b=b, mat=0, k=_lib.DCT_FWD),
+               _lib.op("STORE", a=0, arr=1)]
+        P.nops = len(ops)
+        for i, o in enumerate(ops):
+            P.ops[i] = o
+        return P
+
+    inst = _lib.PgxInstance()
+    for P in (prog(fft_n=0), prog(fft_n=1), prog(nthreads=1024), prog(b=2, nslots=1)):
+        assert L.pgx_run(ctypes.byref(P), ctypes.byref(inst), None) == 1   # PGX_E_ARG
+    assert _lib.MAX_THREADS == 1024 and _lib.MAX_THREADS_FFT == 768
