@@ -1,8 +1,8 @@
 """Fields in physical and spectral space on the GPU (pypde/field.py).
 
 ``v`` and ``vhat`` are float64 CUDA tensors; assigning a NumPy array moves it
-to the device.  HDF5 I/O and plotting are not part of the time-step path and
-are not provided.
+to the device.  ``write`` / ``read`` keep the reference's snapshot layout
+(``io.py``); plotting is not provided.
 """
 import numpy as np
 import torch
@@ -153,6 +153,20 @@ class Field(SpectralSpace, FieldBase):
         self.V.append(self.v.clone())
         self.T.append(self.t)
 
+    def write(self, filename="file_0.h5", dict=None, leading_str="flow", add_time=True,  # noqa: A002
+              grp_name=""):
+        """field.py:83-117: v, vhat, time, x, y (and ``dict``) into the snapshot file."""
+        from . import io
+        with io.Store(io.snapshot_name(self.t, filename, leading_str, add_time), "a") as st:
+            io.write_field(self, st, grp_name, dict)
+
+    def read(self, filename="file_0.h5", dict=None, leading_str="flow", add_time=True,  # noqa: A002
+             grp_name=""):
+        """field.py:137-173: v, vhat, time (and the ``dict`` keys, filled in place)."""
+        from . import io
+        with io.Store(io.snapshot_name(self.t, filename, leading_str, add_time), "r") as st:
+            io.read_field(self, st, grp_name, dict)
+
 
 class FieldBC(SpectralSpaceBC, FieldBase):
     """Inhomogeneous boundary-condition field (field.py:359-414)."""
@@ -186,6 +200,23 @@ class MultiField:
     def save(self):
         for f in self.fields:
             f.save()
+
+    def write(self, filename=None, leading_str="", add_time=True, dict={}):  # noqa: A002, B006
+        """field.py:450-459: every field in its group of one snapshot file."""
+        from . import io
+        name = io.snapshot_name(self.fields[0].t, filename, leading_str, add_time)
+        with io.Store(name, "a") as st:
+            for f, n in zip(self.fields, self.names):
+                io.write_field(f, st, n, dict)
+        return io.container_path(name)
+
+    def read(self, filename=None, leading_str="", add_time=True, dict={}):  # noqa: A002, B006
+        """field.py:440-448."""
+        from . import io
+        name = io.snapshot_name(self.fields[0].t, filename, leading_str, add_time)
+        with io.Store(name, "r") as st:
+            for f, n in zip(self.fields, self.names):
+                io.read_field(f, st, n, dict)
 
     def update_time(self, dt):
         for f in self.fields:

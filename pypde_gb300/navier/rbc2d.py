@@ -306,6 +306,26 @@ class NavierStokes(NavierStokesBase, NavierStokesSteadyState, Integrator):
                 if callback:
                     self.callback()
 
+    # -- snapshots in the reference's layout (rbc2d_base.py:208-228)
+    def write(self, filename=None, leading_str="", add_time=True):
+        """temp / ux / uy / pres groups with v, vhat; time, x, y, nu, kappa, ra, pr at the root.
+        Returns the path written."""
+        L = float(self.y[-1] - self.y[0])
+        meta = {"nu": self.nu, "kappa": self.kappa, "ra": 1.0 / (self.nu * self.kappa) * L ** 3.0,
+                "pr": self.nu / self.kappa}
+        return self.field.write(filename=filename, leading_str=leading_str, add_time=add_time, dict=meta)
+
+    def read(self, filename=None, leading_str="", add_time=True):
+        """Fields, time, ra and pr from a snapshot; the solver plans are rebuilt for them."""
+        meta = {"ra": self.ra, "pr": self.pr}
+        self.field.read(filename=filename, leading_str=leading_str, add_time=add_time, dict=meta)
+        self.time = self.field.fields[0].t
+        self.CONFIG.update({k: float(v) for k, v in meta.items()})
+        self.__dict__.update(**self.CONFIG)
+        self.set_nu_kappa()
+        self.setup_solver()
+        self._fused = None
+
     # -- state as host arrays
     def state(self):
         return {k: to_host(getattr(self, k).vhat) for k in ("T", "U", "V", "P", "pres")}

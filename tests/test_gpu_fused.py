@@ -367,3 +367,23 @@ def test_iterate_fused_matches_update_loop(NS):
     assert abs(ta - tb) < 1e-12 and ca == cb and len(ca) == 4
     for k in a:
         assert rel_err(b[k], a[k]) < 1e-11, k
+
+
+def test_snapshot_write_read_continues_the_run(NS, tmp_path):
+    """NavierStokes.write / read (rbc2d_base.py:208-228): a solver read from the snapshot of another
+    (different Ra / Pr on construction) holds its fields, time, Ra and Pr and steps identically."""
+    a = NS(case="linear", shape=(33, 33), ra=3e4, pr=0.7, dt=0.01, dealias=True, integrator="eu", tsave=None)
+    a.set_temperature_noise(5, 1e-2)
+    a.iterate(0.05)
+    path = a.write(filename=str(tmp_path / "snap.h5"))
+    b = NS(case="linear", shape=(33, 33), ra=1e5, pr=1.0, dt=0.01, dealias=True, integrator="eu", tsave=None)
+    b.read(filename=str(tmp_path / "snap.h5"))
+    assert path.startswith(str(tmp_path))
+    assert abs(b.ra - 3e4) < 1e-6 * 3e4 and abs(b.pr - 0.7) < 1e-12 and abs(b.time - a.time) < 1e-12
+    for k, v in a.state().items():
+        if k != "P":
+            assert np.array_equal(b.state()[k], v), k
+    a.update()
+    b.update()
+    for k in ("T", "U", "V"):
+        assert rel_err(b.state()[k], a.state()[k]) < 1e-12, k
