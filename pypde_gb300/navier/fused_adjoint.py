@@ -41,8 +41,8 @@ import torch
 
 from .. import _lib
 from .._dev import DTYPE, device, to_dev
-from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_DT, P_EDT, P_EDU, P_IDT, P_ISX, P_ISZ, P_MDT, P_MDTSX,
-                    P_MDTSZ, P_MNU, P_TF, FusedBatch, Prog, _Instance, build_programs, host_tables)
+from .fused import (L_M, L_MD, L_MG, L_N, L_ND, L_NG, P_B, P_C, P_DT, P_EDT, P_EDU, P_IDT, P_ISX, P_ISZ, P_MDT,
+                    P_MDTSX, P_MDTSZ, P_MNU, P_TF, FusedBatch, Prog, _Instance, build_programs, host_tables)
 
 BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
@@ -76,10 +76,16 @@ def _explicit_diffusion_y_t():
     return p
 
 
-def build_adjoint_programs(tkind, fft, split=False, beta=False):
+def build_adjoint_programs(tkind, fft, split=False, beta=False, rk3=False):
     """R1 and the thirteen transposed passes of one IMEX Euler step; R1 is the forward P1 of
     the same form (``split``: per-field) as the batch's forward passes.  ``beta``: with the
-    transposes of the explicit-diffusion terms (Q3 / Q3r and the extra pass Q2e)."""
+    transposes of the explicit-diffusion terms (Q3 / Q3r and the extra pass Q2e).
+
+    ``rk3``: the passes of one stage k of the three-stage step.  The stage's products use the
+    velocity w = b_k u_k + c_k u_(k-1) (rbc2d_base.py:86-102): Q2u forms it from this stage's
+    velocity and the previous stage's (UXO, UZO), and Q2z splits the gradient on w into
+    b_k (u_k's own path, plus the carried c_(k+1) part from stage k+1, bUXC / bUZC) and c_k
+    (stored for stage k-1, bUXO / bUZO)."""
     BWD, BWD_T, FWD_T = _lib.DCT_BWD, _lib.DCT_BWD_T, _lib.DCT_FWD_T
     kinds = {"U": "CD", "V": "CD", "T": tkind}
     ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
@@ -253,6 +259,10 @@ def build_adjoint_programs(tkind, fft, split=False, beta=False):
         p.stencil(s, "CD")
         p.setlen(s, L_MD)
     p.dct(0, BWD, fft, count=2)
+    if rk3:
+        for s_, O in ((0, "UXO"), (1, "UZO")):
+            p.scale(s_, par=P_B)
+            p.load_add(s_, O, par=P_C)
     p.store(0, "UXP")
     p.store(1, "UZP")
     p.load(0, "bDPZ", L_M)
@@ -305,11 +315,16 @@ def build_adjoint_programs(tkind, fft, split=False, beta=False):
     p.load(0, "bX_U", L_MD)
     p.load_add(0, "bX_V")
     p.load_add(0, "bX_T")
+    if rk3:
+        p.add("STORE", 0, arr="bXO", par=P_C)     # c_k part: the previous stage's velocity
+        p.scale(0, par=P_B)
+        p.load_add(0, "bXC")                      # + the next stage's c_(k+1) part on this velocity
     p.dct(0, BWD_T, fft)
     p.setlen(0, L_M)
     p.stencil_t(0, "CD")
     p.store_add(0, "bA_X0")
-    p.variants = [{"arrays": {"bX_U": X + "U", "bX_V": X + "V", "bX_T": X + "T", "bA_X0": "bA_" + F + "0"}}
+    p.variants = [{"arrays": {"bX_U": X + "U", "bX_V": X + "V", "bX_T": X + "T", "bA_X0": "bA_" + F + "0",
+                              "bXO": X[:-1] + "O", "bXC": X[:-1] + "C"}}
                   for X, F in (("bUX_", "U"), ("bUZ_", "V"))]
     Q.append(p)
 
@@ -331,9 +346,15 @@ def build_adjoint_programs(tkind, fft, split=False, beta=False):
     return Q
 
 
-def adjoint_shapes(N, M, Nd, Md, beta=False):
-    """Intermediate arrays of the adjoint passes (name -> shape)."""
+def adjoint_shapes(N, M, Nd, Md, beta=False, rk3=False):
+    """Intermediate arrays of the adjoint passes (name -> shape); ``rk3``: with the velocity
+    gradients carried between stages (bUX_0 / bUX_1 for u_0 / u_1, a sink for stage 0's zero
+    part and a zero input for stage 2)."""
     sh = {}
+    if rk3:
+        for X in ("bUX_", "bUZ_"):
+            for k in ("0", "1", "S", "Z"):
+                sh[X + k] = (Nd, Md)
     if beta:
         for F in "UVT":
             sh["bEY0_" + F] = (N - 2, M)
@@ -355,6 +376,12 @@ def adjoint_shapes(N, M, Nd, Md, beta=False):
     return sh
 
 
+# stage k of the reverse RK3 step: carried gradient on its own velocity (C) and on the previous one (O)
+RK3_CARRY = ({"bUXC": "bUX_0", "bUZC": "bUZ_0", "bUXO": "bUX_S", "bUZO": "bUZ_S"},
+             {"bUXC": "bUX_1", "bUZC": "bUZ_1", "bUXO": "bUX_0", "bUZO": "bUZ_0"},
+             {"bUXC": "bUX_Z", "bUZC": "bUZ_Z", "bUXO": "bUX_1", "bUZO": "bUZ_1"})
+
+
 def add_adjoint_buffers(I, bar_views, beta=False):
     """Gradient arrays, scratch and transposed operator tables of one instance."""
     ns = I.ns
@@ -363,8 +390,12 @@ def add_adjoint_buffers(I, bar_views, beta=False):
     a = I.arrays
     for k in BAR_STATE:
         a[k] = bar_views[k]
-    for k, shp in adjoint_shapes(N, M, Nd, Md, beta).items():
+    rk3 = I.nstage == 3
+    for k, shp in adjoint_shapes(N, M, Nd, Md, beta, rk3).items():
         a[k] = torch.zeros(shp, dtype=DTYPE, device=dev)
+    if rk3:
+        for st, carry in zip(I.stage_arrays, RK3_CARRY):
+            st.update(carry)
     host = host_tables(N, M, ns.T.xs[0].id, ns.dt * float(ns.beta), ns.nu, ns.kappa, ns.scale, ns.solver_P._fd,
                        adjoint=True)
     for k in ("BxT", "ByT", "BSx_UT", "BSx_TT", "BSyT", "HyT", "QyT"):
@@ -381,8 +412,6 @@ class FusedAdjoint(FusedBatch):
     """
 
     def __init__(self, solvers, split=None):
-        if any(ns.nstage != 1 for ns in solvers):
-            raise NotImplementedError("the reverse-mode fused step covers IMEX Euler")
         FusedBatch.__init__(self, solvers, split=split)
         self.bar_arena = torch.zeros_like(self.state_arena)
         off = 0
@@ -394,19 +423,44 @@ class FusedAdjoint(FusedBatch):
                 off += r * c
             add_adjoint_buffers(I, views, self.beta)
         tkind = self.solvers[0].T.xs[0].id
-        self.aprogs = build_adjoint_programs(tkind, self.fft, self.split, self.beta)
-        self.alaunches = [self._pass_launches(p) for p in self.aprogs]
+        self.aprogs = build_adjoint_programs(tkind, self.fft, self.split, self.beta, rk3=self.nstage == 3)
+        # per stage (RK3: its parameters, ADI tables and carried velocity gradients)
+        self.alaunches_st = [[self._pass_launches(p, stage=k) for p in self.aprogs] for k in range(self.nstage)]
+        self.alaunches = self.alaunches_st[0]
+        self._snap = torch.zeros((2, self.state_arena.numel()), dtype=DTYPE, device=self.state_arena.device) \
+            if self.nstage == 3 else None
         self.agraph = None
 
-    def run_adjoint_pass(self, i):
-        for L in self.alaunches[i]:
+    def run_adjoint_pass(self, i, stage=0):
+        for L in self.alaunches_st[stage][i]:
             self._run_launch(L)
 
     def adjoint_step_eager(self, recompute=True):
         """The reverse-mode passes; ``recompute=False`` skips R1 when the caller has put the
-        step's P1 outputs (``a_arena``) in place itself."""
+        step's P1 outputs (``a_arena``) in place itself (IMEX Euler)."""
+        if self.nstage == 3:
+            self._adjoint_step_rk3()
+            return
         for i in range(0 if recompute else 1, len(self.alaunches)):
             self.run_adjoint_pass(i)
+
+    def _adjoint_step_rk3(self):
+        """Reverse of one three-stage step from its input X0 (state_arena, restored at the end):
+        stages 0 and 1 run forward again (their outputs X1, X2; UX_A / UZ_A keep u_0 and UX_B / UZ_B
+        u_1, since stage 2 is not rerun), then stages 2, 1, 0 run backward, each from its own input
+        state (R1 recomputes the stage's P1 outputs)."""
+        npass = len(self.progs)
+        self._snap[0].copy_(self.state_arena)
+        for i in range(npass):
+            self.run_pass(i)
+        self._snap[1].copy_(self.state_arena)
+        for i in range(npass, 2 * npass):
+            self.run_pass(i)
+        for k in (2, 1, 0):
+            if k < 2:
+                self.state_arena.copy_(self._snap[k])
+            for i in range(len(self.aprogs)):
+                self.run_adjoint_pass(i, k)
 
     def adjoint_step(self):
         if self.agraph is not None:
@@ -416,12 +470,15 @@ class FusedAdjoint(FusedBatch):
 
     @property
     def adjoint_launches_per_step(self):
-        return sum(len(g) for g in self.alaunches)
+        n = sum(len(g) for st in self.alaunches_st for g in st)
+        if self.nstage == 3:  # the forward recomputation of stages 0 and 1
+            n += sum(len(g) for g in self.launches[:2 * len(self.progs)])
+        return n
 
     def autotune_adjoint(self, reps=3, verbose=False):
         """Tile choice for every launch of the adjoint passes (state and gradients restored after)."""
         saved_s, saved_b = self.state_arena.clone(), self.bar_arena.clone()
-        chosen = self._tune(self.alaunches, reps, verbose)
+        chosen = self._tune([g for st in self.alaunches_st for g in st], reps, verbose)
         self.state_arena.copy_(saved_s)
         self.bar_arena.copy_(saved_b)
         torch.cuda.synchronize()
@@ -482,8 +539,10 @@ class HorizonGradient:
         z = lambda *shape: torch.zeros(shape, dtype=DTYPE, device=dev)  # noqa: E731
         self.ckpt = z(self.nseg, n)
         # per step of a segment: the P1 outputs (physical-space operands of the convection terms),
-        # which is all the reverse-mode passes read of the forward state
-        self.traj = z(2 if overlap else 1, every, fa.a_arena.numel())
+        # which is all the reverse-mode passes of an Euler step read of the forward state; for RK3
+        # the step's input state (its reverse recomputes the stages from it)
+        self.rk3 = fa.nstage == 3
+        self.traj = z(2 if overlap else 1, every, n if self.rk3 else fa.a_arena.numel())
         self.x0, self.x_in, self.g_out, self.y_out, self.g_in = z(n), z(n), z(n), z(n), z(n)
         self.J_out = z(len(fa.insts))
         self._mask = z(n)
@@ -526,10 +585,16 @@ class HorizonGradient:
         return J, r * scale
 
     def _recompute(self, batch, s, buf):
-        """P1 outputs of every step of segment s into traj[buf] (batch: a working set)."""
+        """P1 outputs (RK3: input states) of every step of segment s into traj[buf] (batch: a
+        working set)."""
         k = self._seg_len(s)
         batch.state_arena.copy_(self.ckpt[s])
         for j in range(k):
+            if self.rk3:
+                self.traj[buf, j].copy_(batch.state_arena)
+                if j + 1 < k:
+                    batch.step_eager()
+                continue
             if j + 1 < k:
                 batch.step_eager()
             else:
@@ -539,8 +604,12 @@ class HorizonGradient:
     def _reverse(self, s, buf):
         fa = self.fa
         for j in reversed(range(self._seg_len(s))):
-            fa.a_arena.copy_(self.traj[buf, j])
-            fa.adjoint_step_eager(recompute=False)
+            if self.rk3:
+                fa.state_arena.copy_(self.traj[buf, j])
+                fa.adjoint_step_eager()
+            else:
+                fa.a_arena.copy_(self.traj[buf, j])
+                fa.adjoint_step_eager(recompute=False)
 
     def _reverse_sweep(self):
         if not self.overlap:

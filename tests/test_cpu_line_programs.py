@@ -264,3 +264,85 @@ def test_beta_split_matches_fused():
         out.append({k: m.arrays[k].copy() for k in STATE})
     for k in STATE:
         assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * np.abs(out[0][k]).max(), k
+
+
+def _rk3_machines(N, M, tk, seed):
+    """Three stage views of one instance (rbc2d_base.py:86-102 coefficients): shared arrays, per
+    stage its parameters, ADI tables, velocity arrays (UXC / UXO) and carried velocity gradients."""
+    from pypde_gb300.navier.fused_adjoint import RK3_CARRY
+    m, rng = make_machine(N, M, tk, True, seed)
+    Nd, Md = m.lens[5], m.lens[6]
+    for k in ("UX_A", "UX_B", "UZ_A", "UZ_B"):
+        m.arrays[k] = np.zeros((Nd, Md))
+    for k, shp in adjoint_shapes(N, M, Nd, Md, rk3=True).items():
+        m.arrays.setdefault(k, np.zeros(shp))
+    ra, pr, dt, aspect = 3e4, 1.0, 0.01, 1.5
+    nu, kappa, scale = np.sqrt(pr / ra), np.sqrt(1.0 / pr / ra), (aspect * 0.5, 0.5)
+    a, b, c = (8 / 15, 2 / 15, 1 / 3), (8 / 15, 5 / 12, 3 / 4), (0.0, -17 / 60, -5 / 12)
+
+    def mats(n):
+        return stencil_matrix("CN", n), pseudoinverse_d2(n)[2:, :], np.eye(n)[2:, :]
+
+    fd = poisson2d_matrices(mats(N), mats(M), True, scale)
+    out = []
+    for k in range(3):
+        par = instance_params(N, M, True, dt, nu, kappa, scale, a[k], b[k], c[k])[1]
+        tables = dict(m.tables)
+        tables.update({t: v for t, v in host_tables(N, M, tk, dt * a[k], nu, kappa, scale, fd).items()
+                       if t in ("Ax_U", "Ax_T", "Ay_U", "Ay_T")})
+        cur, old = ("A", "A") if k == 0 else (("B", "A") if k == 1 else ("A", "B"))
+        alias = {"UXC": "UX_" + cur, "UZC": "UZ_" + cur, "UXO": "UX_" + old, "UZO": "UZ_" + old, **RK3_CARRY[k]}
+        arrays = dict(m.arrays)
+        for name, target in alias.items():
+            arrays[name] = m.arrays[target]          # the same array object: in-place updates shared
+        out.append(Machine(arrays, tables, m.lens, par))
+    return out, m.arrays, rng
+
+
+@pytest.mark.parametrize("tk", ["CD", "CN"])
+def test_rk3_adjoint_is_the_transposed_step(tk):
+    """The reverse RK3 step (stages 0, 1 rerun; stages 2, 1, 0 backward with the velocity gradients
+    carried between stages) is the transpose of the three-stage step's linearisation."""
+    st, arrays, rng = _rk3_machines(12, 13, tk, 7)
+    fwd = build_programs(tk, True, rk3=True)
+    adj = build_adjoint_programs(tk, True, rk3=True)
+    keys = STATE + ("PG",)
+    X = {k: 1e-1 * rng.standard_normal(arrays[k].shape) for k in keys}
+    d = {k: rng.standard_normal(arrays[k].shape) for k in STATE}
+    g = {k: rng.standard_normal(arrays[k].shape) for k in STATE}
+
+    def phi(Y):
+        for k in keys:
+            arrays[k][...] = Y[k]
+        for mk in st:
+            for p in fwd:
+                mk.run(p)
+        return {k: arrays[k].copy() for k in STATE}
+
+    def cd(h):   # central difference of <g, Phi(X + h d)>
+        yp = phi({k: X[k] + h * d.get(k, 0.0) for k in keys})
+        ym = phi({k: X[k] - h * d.get(k, 0.0) for k in keys})
+        return sum(float((g[k] * (yp[k] - ym[k])).sum()) / (2 * h) for k in STATE)
+
+    # the three-stage step is not quadratic: Richardson extrapolation removes the O(h^2) term
+    lhs = (4.0 * cd(5e-5) - cd(1e-4)) / 3.0
+    for k in keys:
+        arrays[k][...] = X[k]
+    for k in STATE:
+        arrays["b" + k][...] = g[k]
+    arrays["bPG"][...] = 0.0
+    snap = []
+    snap.append({k: arrays[k].copy() for k in keys})
+    for p in fwd:
+        st[0].run(p)
+    snap.append({k: arrays[k].copy() for k in keys})
+    for p in fwd:
+        st[1].run(p)
+    for k in (2, 1, 0):
+        if k < 2:
+            for key in keys:
+                arrays[key][...] = snap[k][key]
+        for p in adj:
+            st[k].run(p)
+    rhs = sum(float((arrays["b" + k] * d[k]).sum()) for k in STATE)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)

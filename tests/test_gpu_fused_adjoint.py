@@ -258,3 +258,60 @@ def test_horizon_gradient_groups_match_one_batch(torch):
             for key, v in fa_g.views(g)[k].items():
                 assert rel_err(v.cpu().numpy(), ref[key].cpu().numpy()) < 1e-11, (i, key)
             i += 1
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["fused", "per-field"])
+@pytest.mark.parametrize("case,beta", [("linear", 1.0), ("rbc", 1.0), ("linear", 0.5)])
+def test_adjoint_step_rk3_vs_autograd(torch, case, beta, split):
+    """The reverse three-stage step (stages 0, 1 rerun, stages 2, 1, 0 backward with the velocity
+    gradients carried between stages) against the autograd VJP of the plain RK3 step."""
+    from pypde_gb300.navier.adjoint import step
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint
+    ns = _ns(case, (33, 33), integrator="rk3", beta=beta)
+    X = _random_state(torch, ns, 25)
+    rng = np.random.default_rng(26)
+    gbar = [torch.as_tensor(rng.standard_normal(tuple(x.shape)), device="cuda") for x in X]
+    Xr = [x.clone().requires_grad_(True) for x in X]
+    with torch.enable_grad():
+        Y = step(ns, Xr)
+        ref = torch.autograd.grad(Y, Xr, gbar)
+    ns2 = _ns(case, (33, 33), integrator="rk3", beta=beta)
+    for (k, f), x in zip(KEYS, X):
+        getattr(ns2, f).vhat = x.clone()
+    fa = FusedAdjoint([ns2], split=split)
+    assert fa.nstage == 3 and len(fa.alaunches_st) == 3
+    sv = fa.views(fa.state_arena, keys=("UG", "VG", "TG", "PRES"))[0]
+    x0 = {k: sv[k].clone() for k in sv}
+    bv = fa.views(fa.bar_arena, keys=("UG", "VG", "TG", "PRES"))[0]
+    for (k, _), g in zip(KEYS, gbar):
+        bv[k].copy_(g)
+    fa.adjoint_step_eager()
+    for k in sv:                               # the step's input is left in place
+        assert torch.equal(sv[k], x0[k]), k
+    for (k, _), r in zip(KEYS, ref):
+        e = rel_err(bv[k].cpu().numpy(), r.cpu().numpy())
+        assert e < 1e-10, (k, e)
+
+
+def test_horizon_gradient_rk3_vs_autograd_and_fd(torch):
+    from pypde_gb300.navier.adjoint import ResidualObjective, random_directions
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    H, every = 8, 3
+    ns = _ns("linear", (33, 33), integrator="rk3")
+    X = _random_state(torch, ns, 13)[:3]
+    J_ref, g_ref = ResidualObjective(ns, H, every).value_and_grad(X)
+    fa = FusedAdjoint([_ns("linear", (33, 33), integrator="rk3")])
+    fa.capture(1)
+    fa.capture_adjoint()
+    hg = HorizonGradient(fa, H, every)
+    Xa = _arena_state(torch, fa, [X])
+    J, g = hg.value_and_grad(Xa)
+    assert abs(float(J[0]) - J_ref) / J_ref < 1e-10
+    gv = fa.views(g)[0]
+    for k, r in zip(("TG", "UG", "VG"), g_ref):
+        assert rel_err(gv[k].cpu().numpy(), r.cpu().numpy()) < 1e-9, k
+    for d in random_directions([x.shape for x in X], 2, seed=31, device="cuda"):
+        Da = _arena_state(torch, fa, [d])
+        fd = (float(hg.value(Xa + 1e-6 * Da)[0]) - float(hg.value(Xa - 1e-6 * Da)[0])) / 2e-6
+        ad = float((g * Da).sum())
+        assert abs(fd - ad) / abs(ad) < 1e-6, (fd, ad)
