@@ -1,4 +1,4 @@
-"""Fused Rayleigh-Benard step: ten line-program passes per IMEX Euler step.
+"""Fused Rayleigh-Benard step: eleven line-program passes per IMEX Euler step.
 
 The plain path (``NavierStokes.update``) launches one kernel per pypde
 operation (~150 launches per step).  Here the same step is regrouped into
@@ -11,8 +11,8 @@ the reference's sequence (rbc2d.py:396-434) are grouped per axis:
   P1  x  S_x, D_x, pad, DCT^-1 of U, V, T          -> A_F0, A_Fx   (Nd x M-2)
   P2  y  S_y, D_y, pad, DCT^-1; ux, uz; products;  -> C_F          (Nd x M)
          forward DCT_y + unpad; D_y pres; S_y T
-  P3  x  forward DCT_x + unpad; rhs (pressure, buoyancy, BC terms); B_x;
-         A_x^-1 (ADI x-sweep); old terms B_x S_x F    -> Q1_F, Q2_F
+  P3  x  forward DCT_x + unpad; rhs (pressure, buoyancy, BC terms) -> RHS_F
+  P3s x  B_x; A_x^-1 (ADI x-sweep); old terms B_x S_x F    -> Q1_F, Q2_F
   P4  y  B_y Q1 + B_y S_y Q2; A_y^-1 -> U*, V*, T^{n+1}; S_y U*, D_y S_y V*
   P5  x  divergence; pres -= nu div; B_x div              -> R1
   P6  y  H_y (fast-diagonalisation rhs)                   -> R2
@@ -22,7 +22,7 @@ the reference's sequence (rbc2d.py:396-434) are grouped per axis:
   P10 y  (S^T S)^-1 S^T (y); U = U* - G1, V = V* - G2
 
 A batch of independent instances (any sizes, any Rayleigh numbers) runs the
-same ten launches: every CTA picks (instance, tile) from a work list, so one
+same eleven launches: every CTA picks (instance, tile) from a work list, so one
 launch per pass covers all instances.  ``capture()`` records the passes of a
 step in a CUDA graph.
 """
@@ -229,25 +229,42 @@ def _split_convection_programs(tkind, fft, rk3, beta=False):
     p.variants = [{"arrays": {"C_F": "C_" + F, "RHS_F": "RHS_" + F}} for F in "UVT"]
     P.append(p)
 
-    p = Prog("P3r", 0, L_M, 2)
-    p.load(0, "PRES", L_N)
-    p.diff(0)
-    p.store_add(0, "RHS_U", par=P_MDTSX)
-    p.load(0, "DPZ", L_N, par=P_MDTSZ)
-    p.load_add(0, "TBCC", par=P_DT)
-    p.load(1, "TSY", L_NG)
-    p.stencil(1, tkind)
-    p.axpy(0, 1, par=P_DT)
-    p.store_add(0, "RHS_V")
-    p.load(0, "DTB2", L_N, par=P_DTK)
-    p.store_add(0, "RHS_T")
+    # P3rs (x, lines M): the non-convective right-hand-side terms, then B_x and the ADI x-sweeps
+    # (the same axis and lines: one pass)
+    p = Prog("P3rs", 0, L_M, 6)
+    for i, F in enumerate("UVT"):
+        p.load(i, "RHS_" + F, L_N)
+    p.load(3, "PRES", L_N)
+    p.diff(3)
+    p.axpy(0, 3, par=P_MDTSX)
+    p.load_add(1, "DPZ", par=P_MDTSZ)
+    p.load_add(1, "TBCC", par=P_DT)
+    p.load(3, "TSY", L_NG)
+    p.stencil(3, tkind)
+    p.axpy(1, 3, par=P_DT)
+    p.load_add(2, "DTB2", par=P_DTK)
     if beta:
-        p.nslots = 3
-        for F in "UVT":
-            _explicit_diffusion_x(p, 0, F, kinds[F])
-            p.store_add(0, "RHS_" + F, par=P_EDT if F == "T" else P_EDU)
+        for i, F in enumerate("UVT"):
+            _explicit_diffusion_x(p, 3, F, kinds[F])
+            p.axpy(i, 3, par=P_EDT if F == "T" else P_EDU)
+    _adi_x(p, kinds)
     P.append(p)
     return P
+
+
+def _adi_x(p, kinds):
+    """B_x on the right-hand sides in slots 0-2 and the ADI x-sweep of them and of the old-time
+    terms B_x S_x F (slots 3-5): the six independent sweeps as one multi-slot chain op; stores
+    Q1_F, Q2_F."""
+    ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
+    for i, F in enumerate("UVT"):
+        p.banded(i, "Bx", 0, 3, L_NG)
+        p.load(3 + i, F + "G", L_NG)
+        p.banded(3 + i, "BSx_T" if F == "T" else "BSx_U", -2, 4, L_NG)
+    p.fdma(0, [ax[F] for F in "UVT"] + [ax[F] for F in "UVT"])
+    for i, F in enumerate("UVT"):
+        p.store(i, "Q1_" + F)
+        p.store(3 + i, "Q2_" + F)
 
 
 def _explicit_diffusion_y():
@@ -291,7 +308,7 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
 
     ``split``: P1 - P3 as per-field programs run as three descriptors of one launch
     (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3r (the non-convective
-    right-hand-side terms): the same transforms in twelve passes, with three times
+    right-hand-side terms, with the x-sweeps: P3rs): the same transforms in eleven passes, with three times
     the CTAs in the transform-heavy ones - for batches of few instances.
 
     ``beta``: diffusion beta-implicit (beta != 1, rbc2d.py:268-283, 390-391): the ADI tables and the
@@ -361,9 +378,10 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
         p.store(2, "TSY")
         P.append(p)
 
-        # P3 (x, lines M): forward x-transform and right-hand sides
         if beta:
             P.append(_explicit_diffusion_y())
+        # P3 (x, lines M): forward x-transform, right-hand sides; P3s: B_x and the ADI x-sweeps (as
+        # one pass with P3 the batch ran 2 % slower: more shared memory, fewer CTAs per SM)
         p = Prog("P3", 0, L_M, 5 if beta else 4)
         for i, F in enumerate("UVT"):
             p.load(i, "C_" + F, L_ND)
@@ -388,21 +406,11 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
                 p.axpy(i, 3, par=P_EDT if F == "T" else P_EDU)
             p.store(i, "RHS_" + F)
         P.append(p)
-
-    # P3s (x, lines M): B_x, ADI x-sweep of the rhs and of the old-time terms B_x S_x F;
-    # the six independent sweeps run as one multi-slot chain op
-    p = Prog("P3s", 0, L_M, 6)
-    ax = {"U": "Ax_U", "V": "Ax_U", "T": "Ax_T"}
-    for i, F in enumerate("UVT"):
-        p.load(i, "RHS_" + F, L_N)
-        p.banded(i, "Bx", 0, 3, L_NG)
-        p.load(3 + i, F + "G", L_NG)
-        p.banded(3 + i, "BSx_T" if F == "T" else "BSx_U", -2, 4, L_NG)
-    p.fdma(0, [ax[F] for F in "UVT"] + [ax[F] for F in "UVT"])
-    for i, F in enumerate("UVT"):
-        p.store(i, "Q1_" + F)
-        p.store(3 + i, "Q2_" + F)
-    P.append(p)
+        p = Prog("P3s", 0, L_M, 6)
+        for i, F in enumerate("UVT"):
+            p.load(i, "RHS_" + F, L_N)
+        _adi_x(p, kinds)
+        P.append(p)
 
     # P4 (y, lines N-2): B_y, ADI y-sweep -> U*, V*, T; divergence pieces
     p = Prog("P4", 1, L_NG, 4)

@@ -27,7 +27,9 @@ one launch, which triples the CTAs of a single instance.
   Q5  x  B_x^T, -nu pres-bar, divergence^T           -> W1bar, W2bar
   Q4  y  S_y^T, D_y^T, A_y^-T, B_y^T, (B S)_y^T      -> Q1bar, Q2bar
   Q3s x  A_x^-T, B_x^T, (B S)_x^T                    -> RHSbar, Ubar Vbar Tbar (old-time part)
-  Q3  x  forward-DCT_x^T, pressure / buoyancy terms  -> Cbar, DPZbar, TSYbar, pres-bar
+         (per-field form: and the pressure / buoyancy terms^T)
+  Q3  x  forward-DCT_x^T (per-field form: per field); -> Cbar, DPZbar, TSYbar, pres-bar
+         pressure / buoyancy terms^T
   Q2u y  ux, uz (recomputed); D_y^T, S_y^T          -> UXP, UZP, pres-bar, Tbar
   Q2f y  per field: products^T, DCT_y^T chains       -> A_F*bar, uxbar / uzbar parts
   Q2z y  per component: ux / uz bar chains           -> A_U0bar, A_V0bar
@@ -49,12 +51,14 @@ BAR_STATE = ("bUG", "bVG", "bTG", "bPG", "bPRES")
 
 def _explicit_diffusion_x_t(p, s, F, kind, src):
     """Transpose of the x-half of the explicit diffusion (P3): from the right-hand-side gradient
-    ``src``, EY0_F bar = P_ED S_x^T (D_x^T)^2 / sx^2 and EYY_F bar = P_ED S_x^T of it."""
+    in slot ``src``, EY0_F bar = P_ED S_x^T (D_x^T)^2 / sx^2 and EYY_F bar = P_ED S_x^T of it."""
     ed = P_EDT if F == "T" else P_EDU
-    p.load(s, src, L_N, par=ed)
+    p.copy(s, src)
+    p.scale(s, par=ed)
     p.stencil_t(s, kind)
     p.store(s, "bEYY_" + F)
-    p.load(s, src, L_N, par=ed)
+    p.copy(s, src)
+    p.scale(s, par=ed)
     p.scale(s, par=P_ISX)
     p.scale(s, par=P_ISX)
     p.diff_t(s, count=2)
@@ -79,7 +83,7 @@ def _explicit_diffusion_y_t():
 def build_adjoint_programs(tkind, fft, split=False, beta=False, rk3=False):
     """R1 and the thirteen transposed passes of one IMEX Euler step; R1 is the forward P1 of
     the same form (``split``: per-field) as the batch's forward passes.  ``beta``: with the
-    transposes of the explicit-diffusion terms (Q3 / Q3r and the extra pass Q2e).
+    transposes of the explicit-diffusion terms (in Q3s and the extra pass Q2e).
 
     ``rk3``: the passes of one stage k of the three-stage step.  The stage's products use the
     velocity w = b_k u_k + c_k u_(k-1) (rbc2d_base.py:86-102): Q2u forms it from this stage's
@@ -186,7 +190,9 @@ def build_adjoint_programs(tkind, fft, split=False, beta=False, rk3=False):
         p.store(i, "bQ1_" + F)
     Q.append(p)
 
-    # Q3s (x, M lines): Q1 = A_x^-1 B_x RHS; Q2 = A_x^-1 (B S)_x F  (starts the state gradient)
+    # Q3s (x, M lines): Q1 = A_x^-1 B_x RHS; Q2 = A_x^-1 (B S)_x F (starts the state gradient); then,
+    # per-field form, from the RHS gradient in slots 0-2 the transposed right-hand-side terms (the
+    # same axis and lines: one pass); fused form: those terms and the x-transform in Q3
     p = Prog("Q3s", 0, L_M, 6)
     for i, F in enumerate("UVT"):
         p.load(i, "bQ1_" + F, L_NG)
@@ -194,57 +200,46 @@ def build_adjoint_programs(tkind, fft, split=False, beta=False, rk3=False):
     p.fdma_t(0, [ax[F] for F in "UVT"] * 2)
     for i, F in enumerate("UVT"):
         p.banded(i, "BxT", -4, 3, L_N)
-        p.store(i, "bRHS_" + F)
+        p.store(i, "bRHS_" + F)               # read by Q3
         p.banded(3 + i, "BSx_TT" if F == "T" else "BSx_UT", -4, 4, L_NG)
         p.store(3 + i, "b" + F + "G")
+    if not split:  # Q3 (x, M lines): the terms and the forward x-transform, as the forward P3 / P3s
+        Q.append(p)
+        p = Prog("Q3", 0, L_M, 4)
+        for i, F in enumerate("UVT"):
+            p.load(i, "bRHS_" + F, L_N)
+    for i, F in enumerate("UVT"):
+        if beta:
+            _explicit_diffusion_x_t(p, 3, F, kinds[F], i)
+        if F == "U":
+            p.copy(3, i)
+            p.scale(3, par=P_MDTSX)
+            p.diff_t(3)
+            p.store_add(3, "bPRES")
+        elif F == "V":
+            p.copy(3, i)
+            p.scale(3, par=P_MDTSZ)
+            p.store(3, "bDPZ")
+            p.copy(3, i)
+            p.scale(3, par=P_DT)
+            p.stencil_t(3, tkind)
+            p.store(3, "bTSY")
+        if not split:
+            p.scale(i, par=P_MDT)
+            p.setlen(i, L_ND)
+    if not split:
+        p.dct(0, FWD_T, fft, count=3)
+        for i, F in enumerate("UVT"):
+            p.store(i, "bC_" + F)
     Q.append(p)
 
-    # Q3 (x, M lines): RHS = -dt Fwd_x C (+ pressure gradient, buoyancy, lift terms)
-    if split:  # per field (Q3, three descriptors) and the other terms (Q3r)
+    if split:  # Q3 (x, M lines), per field (three descriptors): RHS = -dt Fwd_x C
         p = Prog("Q3", 0, L_M, 1)
         p.load(0, "bRHS_F", L_N, par=P_MDT)
         p.setlen(0, L_ND)
         p.dct(0, FWD_T, fft)
         p.store(0, "bC_F")
         p.variants = [{"arrays": {"bRHS_F": "bRHS_" + F, "bC_F": "bC_" + F}} for F in "UVT"]
-        Q.append(p)
-        p = Prog("Q3r", 0, L_M, 1)
-        p.load(0, "bRHS_U", L_N, par=P_MDTSX)
-        p.diff_t(0)
-        p.store_add(0, "bPRES")
-        p.load(0, "bRHS_V", L_N, par=P_MDTSZ)
-        p.store(0, "bDPZ")
-        p.load(0, "bRHS_V", L_N, par=P_DT)
-        p.stencil_t(0, tkind)
-        p.store(0, "bTSY")
-        if beta:
-            for F in "UVT":
-                _explicit_diffusion_x_t(p, 0, F, kinds[F], "bRHS_" + F)
-        Q.append(p)
-    else:
-        p = Prog("Q3", 0, L_M, 4)
-        for i, F in enumerate("UVT"):
-            if beta:
-                _explicit_diffusion_x_t(p, 3, F, kinds[F], "bRHS_" + F)
-            p.load(i, "bRHS_" + F, L_N)
-            if F == "U":
-                p.copy(3, i)
-                p.scale(3, par=P_MDTSX)
-                p.diff_t(3)
-                p.store_add(3, "bPRES")
-            elif F == "V":
-                p.copy(3, i)
-                p.scale(3, par=P_MDTSZ)
-                p.store(3, "bDPZ")
-                p.copy(3, i)
-                p.scale(3, par=P_DT)
-                p.stencil_t(3, tkind)
-                p.store(3, "bTSY")
-            p.scale(i, par=P_MDT)
-            p.setlen(i, L_ND)
-        p.dct(0, FWD_T, fft, count=3)
-        for i, F in enumerate("UVT"):
-            p.store(i, "bC_" + F)
         Q.append(p)
 
     if beta:

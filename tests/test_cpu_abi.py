@@ -68,9 +68,12 @@ def test_fused_programs_fit_the_abi(tkind, fft):
     slots it declares."""
     from pypde_gb300 import _lib
     from pypde_gb300.navier.fused import build_programs
-    progs = (build_programs(tkind, fft) + build_programs(tkind, fft, rk3=True) +
-             build_programs(tkind, fft, split=True) + build_programs(tkind, fft, rk3=True, split=True))
-    assert len(progs) == 11 + 11 + 13 + 13
+    progs = []
+    for beta in (False, True):
+        progs += (build_programs(tkind, fft, beta=beta) + build_programs(tkind, fft, rk3=True, beta=beta) +
+                  build_programs(tkind, fft, split=True, beta=beta) +
+                  build_programs(tkind, fft, rk3=True, split=True, beta=beta))
+    assert len(progs) == (11 + 11 + 12 + 12) + (12 + 12 + 13 + 13)
     uses_b = {_lib.OP[k] for k in ("AXPY", "MUL", "COPY")}
     for p in progs:
         assert len(p.ops) <= _lib.MAX_OPS, p.name

@@ -72,7 +72,7 @@ def test_adjoint_step_vs_autograd(torch, case, shape, dealias):
 @pytest.mark.parametrize("split", [False, True], ids=["fused", "per-field"])
 @pytest.mark.parametrize("case", ["linear", "rbc"])
 def test_adjoint_step_beta_vs_autograd(torch, case, split):
-    """beta != 1: the reverse-mode passes with the transposed explicit-diffusion terms (Q3 / Q3r, Q2e)."""
+    """beta != 1: the reverse-mode passes with the transposed explicit-diffusion terms (Q3s, Q2e)."""
     from pypde_gb300.navier.adjoint import step
     from pypde_gb300.navier.fused_adjoint import FusedAdjoint
     ns = _ns(case, (33, 33), beta=0.4)
