@@ -9,7 +9,7 @@ from a CUDA graph (``pypde_gb300.navier.fused``).
 import numpy as np
 import torch
 
-from .._dev import to_dev, to_host
+from .._dev import to_host
 from ..bases import Base
 from ..field import Field, FieldBC, MultiField
 from ..field_operations import avg_vol, avg_x, cheby_to_galerkin, convective_term, galerkin_to_cheby, grad
