@@ -949,7 +949,7 @@ def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, dm):
             tb -= tb % 2          # twice the CTAs when an instance has few lines
         if tb < 1 or tb * per_line > SMEM_PER_SM - 2048:
             continue
-        for nt in (256, 512):
+        for nt in (64, 128, 256, 512):
             nt = max(nt, 32 * -(-width * tb // 32))
             if nt <= ntmax and (tb, nt, False, sd, dm) not in out:
                 out.append((tb, nt, False, sd, dm))
