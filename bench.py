@@ -273,7 +273,7 @@ def run_gpu(args, rank, world):
         with open(args.save_tiles, "w") as f:
             json.dump({"forward": fb.tiles()}, f)
     if args.graph_groups:
-        fb.capture(1, groups="shape" if args.graph_groups < 0 else args.graph_groups)
+        fb.capture(1, groups="shape%d" % -args.graph_groups if args.graph_groups < 0 else args.graph_groups)
         group_times = None
     elif args.no_tune:
         fb.capture(1)
@@ -671,7 +671,7 @@ def main():
                     help="instance groups of the batched gradient, each on its own stream (measured on the "
                          "32-instance batch: 1 group 22.5, 4 groups 20.5, 8 groups 17.0 gradients/s)")
     ap.add_argument("--graph-groups", type=int, default=0,
-                    help="instance groups as parallel branches of the step's graph (0: tuned, -1: one "
+                    help="instance groups as parallel branches of the step's graph (0: tuned, -K: K "
                          "per instance shape)")
     ap.add_argument("--e2e-groups", type=int, default=4,
                     help="instance groups of the end-to-end step, each on its own stream")

@@ -1177,11 +1177,15 @@ class FusedBatch:
             for k, v in s.items():
                 I.arrays[k].copy_(v)
         branches = []
-        if groups == "shape":  # one branch per instance shape: every launch of a branch is one size class
+        if isinstance(groups, str) and groups.startswith("shape"):
+            # one branch per instance shape (every launch of a branch is one size class); "shapeK":
+            # each shape's instances in K branches
+            per = int(groups[5:] or 1)
             shapes = {}
             for k, I in enumerate(self.insts):
                 shapes.setdefault((I.N, I.M), []).append(k)
-            branches = [(self._subset(idx), torch.cuda.Stream()) for idx in shapes.values()]
+            parts = [idx[j::per] for idx in shapes.values() for j in range(per) if idx[j::per]]
+            branches = [(self._subset(idx), torch.cuda.Stream()) for idx in parts]
         elif groups > 1:
             branches = [(self._subset(idx), torch.cuda.Stream()) for idx, _, _ in self._split_groups(groups)]
         g = torch.cuda.CUDAGraph()
@@ -1232,24 +1236,26 @@ class FusedBatch:
         sub.launches = [sub._pass_launches(p, None, st, key_tiles) for st in range(sub.nstage) for p in sub.progs]
         return sub
 
-    def tune_groups(self, candidates=(1, 2, 4, 8, 16, "shape"), reps=5):
+    def tune_groups(self, candidates=(1, 2, 4, 8, "shape"), reps=20):
         """Capture the step with each number of instance groups (parallel graph branches), time
         ``reps`` replays of each and keep the fastest ("shape": one branch per instance shape); the
-        state is restored after every trial.  Returns {groups: ms per step}."""
+        state is restored after every trial.  Returns {groups: ms per step}.  (Graphs of 16 or more
+        branches ran slower, and from one capture to the next their time varied by 10 %.)"""
         saved = self.state_arena.clone()
         times = {}
         for G in candidates:
-            if G != "shape" and G > len(self.insts):
+            if not isinstance(G, str) and G > len(self.insts):
                 continue
             self.capture(1, groups=G)
-            self.step()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            for _ in range(reps):
+            for _ in range(3):
                 self.step()
-            b.record()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for a, b in ev:   # an event pair around every replay, as a timed loop records them
+                a.record()
+                self.step()
+                b.record()
             torch.cuda.synchronize()
-            times[G] = a.elapsed_time(b) / reps
+            times[G] = sum(a.elapsed_time(b) for a, b in ev) / reps
             self.state_arena.copy_(saved)
         best = min(times, key=times.get)
         self.capture(1, groups=best)
