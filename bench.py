@@ -311,7 +311,7 @@ def run_gpu(args, rank, world):
     # another's passes
     host = torch.empty(fb.state_arena.numel(), dtype=torch.float64, pin_memory=True)
     host.copy_(fb.state_arena)
-    groups = fb.host_pipeline(args.e2e_groups)
+    groups = fb.host_pipeline(args.e2e_groups, branches=1)
 
     def e2e_step():
         fb.step_host(host)
@@ -673,7 +673,7 @@ def main():
     ap.add_argument("--graph-groups", type=int, default=0,
                     help="instance groups as parallel branches of the step's graph (0: tuned, -K: K "
                          "per instance shape)")
-    ap.add_argument("--e2e-groups", type=int, default=4,
+    ap.add_argument("--e2e-groups", type=int, default=16,
                     help="instance groups of the end-to-end step, each on its own stream")
     ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],
                     help="per-field convection passes (auto: for batches of up to 4 instances)")

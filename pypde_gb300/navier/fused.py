@@ -1187,7 +1187,11 @@ class FusedBatch:
             parts = [idx[j::per] for idx in shapes.values() for j in range(per) if idx[j::per]]
             branches = [(self._subset(idx), torch.cuda.Stream()) for idx in parts]
         elif groups > 1:
-            branches = [(self._subset(idx), torch.cuda.Stream()) for idx, _, _ in self._split_groups(groups)]
+            if self.state_arena is None:   # a launch subset: groups of about equal instance counts
+                parts = [p for p in np.array_split(np.arange(len(self.insts)), groups) if len(p)]
+            else:
+                parts = [idx for idx, _, _ in self._split_groups(groups)]
+            branches = [(self._subset(list(idx)), torch.cuda.Stream()) for idx in parts]
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             cur = torch.cuda.current_stream()
@@ -1272,13 +1276,14 @@ class FusedBatch:
         cuts = sorted(set(min(max(c, 0), len(cum)) for c in cuts))
         return [(range(a, b), starts[a], starts[b]) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
 
-    def host_pipeline(self, groups=2):
+    def host_pipeline(self, groups=2, branches="shape"):
         """Prepare ``step_host``: the instances in ``groups`` contiguous groups of about equal state
-        size, each with its own launch set, CUDA graph and stream."""
+        size, each with its own launch set, CUDA graph (``branches``: its graph branches, as in
+        ``capture``) and stream."""
         self._pipe = []
         for idx, o0, o1 in self._split_groups(groups):
             sub = self._subset(idx)
-            sub.capture(1, groups="shape")
+            sub.capture(1, groups=branches)
             self._pipe.append((sub, o0, o1, torch.cuda.Stream()))
         self._pipe_fresh = True
         return len(self._pipe)
