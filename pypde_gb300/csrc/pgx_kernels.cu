@@ -897,6 +897,63 @@ __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double
   else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, ds, tws);
 }
 
+// The first radix-R stage of the even DCT's FFT (Ns = 1, no twiddles) with the fold computed on
+// its way in: u_m = (x_m + x_{N-m})/2 - sin(pi m/N) (x_m - x_{N-m}) of both lines of every pair,
+// read straight from the slots (no separate fold phase, one barrier fewer per transform).
+template <int R>
+__device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const double2* tw, int N, int nall,
+                                           int npairs, int slot0, const DctScale& ds) {
+  const int LR = N / R;
+  for (int idx = c.tid; idx < nall * LR; idx += c.nthreads) {
+    const int P = idx / LR, j = idx - P * LR;
+    const int sl = P / npairs, pr = P - sl * npairs;
+    const double* x = slot_ptr(c, slot0 + sl);
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int m = j + r * LR;
+      const double sn = -__ldg(&tw[m].y);
+      const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
+      double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
+      double ub = 0.0;
+      if (two) {
+        const double b0 = x[(t0 + 1) * c.lcap + m], b1 = x[(t0 + 1) * c.lcap + N - m];
+        ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
+      }
+      if (ds.has_pre) {
+        const double sg = ds.pre(m, N);
+        ua *= sg;
+        ub *= sg;
+      }
+      v[r] = make_double2(ua, ub);
+    }
+    double2 o[R];
+    if (R == 2) {
+      o[0] = cadd(v[0], v[1]);
+      o[1] = csub(v[0], v[1]);
+    } else if (R == 4) {
+      double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+      double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
+      o[0] = cadd(a, e);
+      o[2] = csub(a, e);
+      o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
+      o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
+    } else {  // R == 3
+      const double h = 0.86602540378443864676;
+      double2 t1 = cadd(v[1], v[2]);
+      double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
+      double2 t3 = csub(v[1], v[2]);
+      o[0] = cadd(v[0], t1);
+      o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));
+      o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[P * c.fft_stride + j * R + q] = o[q];
+  }
+}
+
 // DCT-I for even N = n - 1, exploiting both the realness and the even symmetry
 // of the extension (half the FFT length of the paired approach):
 //   fold   u_j = (x_j + x_{N-j})/2 - sin(pi j/N) (x_j - x_{N-j}),  j = 0..N-1
@@ -923,28 +980,6 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
     return;
   }
-  // fold
-  for (int idx = c.tid; idx < nall * N; idx += c.nthreads) {
-    const int P = idx / N, j = idx - P * N;
-    const int sl = P / npairs, pr = P - sl * npairs;
-    const double* x = slot_ptr(c, op.a + sl);
-    const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
-    const double sn = -__ldg(&tw[j].y);
-    const double sg = ds.has_pre ? ds.pre(j, N) : 1.0;
-    const double a0 = x[t0 * c.lcap + j], a1 = x[t0 * c.lcap + N - j];
-    double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
-    double ub = 0.0;
-    if (two) {
-      const double b0 = x[(t0 + 1) * c.lcap + j], b1 = x[(t0 + 1) * c.lcap + N - j];
-      ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
-    }
-    if (ds.has_pre) {
-      ua *= sg;
-      ub *= sg;
-    }
-    c.f0[P * c.fft_stride + j] = make_double2(ua, ub);
-  }
   // y_1: one warp per line (line lt = sl * tb + t)
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
@@ -964,13 +999,18 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       if (lane == 0) c.ybuf[lt] = fma(2.0 * ps, acc, d0);
     }
   }
-  __syncthreads();
-  // FFT of length N over all pairs
+  // FFT of length N over all pairs (y_1 above and the first stage both only read the slots)
   double2* bufs[2] = {c.f0, c.f1};
   int cur = 0, Ns = 1;
   for (int rem = N; rem > 1;) {
     const int R = next_radix(rem);
-    stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, nall, nullptr, ds, 2);
+    if (Ns == 1) {  // the fold on the way into the first stage
+      if (R == 4) fold_stage<4>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
+      else if (R == 2) fold_stage<2>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
+      else fold_stage<3>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
+    } else {
+      stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, nall, nullptr, ds, 2);
+    }
     cur ^= 1;
     Ns *= R;
     rem /= R;
