@@ -38,7 +38,7 @@ METRIC = "2D RBC FP64 steps/s at 1 GB300: plain vs batched-graph; adjoint grads/
 FP64_PEAK_TFLOPS = 1.256  # measured DFMA throughput of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt)
 # DRAM bytes (read + write) of pass P2 on the 256-instance workload, one ncu capture of its three size-class
 # launches (profiles/line_program_batched_c4_launches.txt)
-P2_DRAM_BYTES = 154.6e6 + 29.1e6
+P2_DRAM_BYTES = 154.6e6 + 27.7e6
 
 
 def workload_specs(kind, n_instances, rank=0):
