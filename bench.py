@@ -26,6 +26,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -152,10 +153,9 @@ class ClockSampler:
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, path=None):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/pgx_bench_clocks.csv"
+        self.path = path or os.path.join(tempfile.gettempdir(), "pgx_bench_clocks.csv")
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
@@ -285,7 +285,7 @@ def run_gpu(args, rank, world):
 
     # warmup + timed region (graph replay), barrier + sync on both sides; the clock sampler starts
     # before the warm-up so that it is producing samples when the timed region begins
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, args.clocks_csv)
     time.sleep(0.5)
     for _ in range(args.warmup):
         fb.step()
@@ -673,6 +673,7 @@ def main():
     ap.add_argument("--graph-groups", type=int, default=0,
                     help="instance groups as parallel branches of the step's graph (0: tuned, -K: K "
                          "per instance shape)")
+    ap.add_argument("--clocks-csv", default=None, help="where the nvidia-smi samples of the timed region go")
     ap.add_argument("--e2e-groups", type=int, default=16,
                     help="instance groups of the end-to-end step, each on its own stream")
     ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],
