@@ -346,7 +346,7 @@ def run_gpu(args, rank, world):
                 "traffic": P2_DRAM_BYTES if (work[dom][0] == "P2" and args.workload == "c4" and n_inst == 256)
                 else None,
                 "peak_source": "measured DFMA peak of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt, "
-                               "pypde_gb300/csrc/fp64_probe.cu); the driver-written peak file carries only HBM and bf16",
+                               "pypde_gb300/csrc/fp64_probe.cu); MEASURED_PEAKS.json carries only HBM and bf16",
                 "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2]}
     step_fl = sum(w[1] for w in work)
     step_fp64 = {"tflops": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12, 4),

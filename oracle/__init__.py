@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY.  This package is a float64 NumPy restatement of the
 reference algorithm (pypde by preiter93) used to check the CUDA path.  Only
 ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may import it, and there only as the checker or as the timed CPU
-baseline.  The product package ``pypde_gb300`` never imports it and has no CPU
+``bench.py`` may import it, and there only as the reference results are compared
+against or as the timed CPU baseline.  The product package ``pypde_gb300`` never imports it and has no CPU
 fallback.
 
 Every function names the reference file:line it restates.  The oracle is

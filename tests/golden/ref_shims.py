@@ -1,8 +1,8 @@
 """Import shims that let the unmodified pypde reference run in this container.
 
 Used only by ``make_golden.py`` (and the reference-pinning CPU test) to run
-the reference itself and record golden vectors.  Nothing here is used on the
-GPU machine or by the product package.
+the reference itself and record golden vectors.  Nothing here is used by the GPU
+tests, the benchmark or the product package.
 
 * The four f2py Fortran modules (differentiate_cheby, tdma, fdma, twodma) are
   restated statement-by-statement from their ``.f90`` sources, with f2py's
