@@ -1099,6 +1099,8 @@ class FusedBatch:
         """Launch descriptors of the forward passes; ``tiles`` = {"pass#group": (lines per CTA,
         threads)} overrides the default choice (e.g. another batch's autotuned tiles)."""
         self.launches = [self._pass_launches(p, tiles, st) for st in range(self.nstage) for p in self.progs]
+        # a graph recorded before reads the old launches' descriptors and work lists: drop it with them
+        self.graph, self.graph_branches = None, []
 
     @staticmethod
     def _tiles_of(launch_sets):
