@@ -1101,6 +1101,7 @@ class FusedBatch:
         self.launches = [self._pass_launches(p, tiles, st) for st in range(self.nstage) for p in self.progs]
         # a graph recorded before reads the old launches' descriptors and work lists: drop it with them
         self.graph, self.graph_branches = None, []
+        self.launch_generation = getattr(self, "launch_generation", 0) + 1
 
     @staticmethod
     def _tiles_of(launch_sets):
@@ -1121,7 +1122,9 @@ class FusedBatch:
 
     def _tune(self, launch_sets, reps, verbose):
         """Time every candidate tile of every launch (each alone) and keep the fastest.
-        The caller saves and restores whatever state the launches modify."""
+        The caller saves and restores whatever state the launches modify.  Graphs recorded over
+        the old launches (here or by a HorizonGradient) see the new ``launch_generation``."""
+        self.launch_generation = getattr(self, "launch_generation", 0) + 1
         stream = torch.cuda.current_stream()
         chosen = {}
         for group in launch_sets:

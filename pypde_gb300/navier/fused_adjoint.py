@@ -458,7 +458,7 @@ class FusedAdjoint(FusedBatch):
                 self.run_adjoint_pass(i, k)
 
     def adjoint_step(self):
-        if self.agraph is not None:
+        if self.agraph is not None and self._agraph_gen == self.launch_generation:
             self.agraph.replay()
         else:
             self.adjoint_step_eager()
@@ -492,7 +492,7 @@ class FusedAdjoint(FusedBatch):
         torch.cuda.synchronize()
         self.state_arena.copy_(saved_s)
         self.bar_arena.copy_(saved_b)
-        self.agraph = g
+        self.agraph, self._agraph_gen = g, self.launch_generation
 
     # -- views of the per-instance state in the arenas
     def views(self, arena, keys=("UG", "VG", "TG")):
@@ -662,7 +662,10 @@ class HorizonGradient:
         if not self.use_graph:
             self._run(what)
             return
-        g = self.graphs.get(what)
+        gen = self.fa.launch_generation
+        g, g_gen = self.graphs.get(what, (None, None))
+        if g is not None and g_gen != gen:   # the batch's launches were rebuilt since: record again
+            g = None
         if g is None:
             saved = (self.ckpt.clone(), self.y_out.clone()) if what == "vjp" else None
             self._run(what)                 # warm-up outside the capture
@@ -673,7 +676,7 @@ class HorizonGradient:
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
                 self._run(what)
-            self.graphs[what] = g
+            self.graphs[what] = (g, gen)
         g.replay()
 
     # ------------------------------------------------------------------- API
