@@ -315,3 +315,23 @@ def test_horizon_gradient_rk3_vs_autograd_and_fd(torch):
         fd = (float(hg.value(Xa + 1e-6 * Da)[0]) - float(hg.value(Xa - 1e-6 * Da)[0])) / 2e-6
         ad = float((g * Da).sum())
         assert abs(fd - ad) / abs(ad) < 1e-6, (fd, ad)
+
+
+def test_horizon_graph_rerecorded_after_retuning(torch):
+    """Retuning the batch replaces its launches; the horizon's recorded graphs are recorded again
+    (a replay of the old ones would read freed descriptors) and give the same gradient."""
+    from pypde_gb300.navier.fused_adjoint import FusedAdjoint, HorizonGradient
+    ns = _ns("linear", (33, 17), ra=2e4)
+    X = _random_state(torch, ns, 40)[:3]
+    fa = FusedAdjoint([_ns("linear", (33, 17), ra=2e4)])
+    hg = HorizonGradient(fa, 6, 3)
+    Xa = _arena_state(torch, fa, [X])
+    J0, g0 = hg.value_and_grad(Xa)
+    gen = fa.launch_generation
+    fa.autotune(reps=1)
+    fa.autotune_adjoint(reps=1)
+    assert fa.launch_generation > gen
+    J1, g1 = hg.value_and_grad(Xa)
+    assert hg.graphs["grad"][1] == fa.launch_generation
+    assert abs(float(J1[0]) - float(J0[0])) <= 1e-13 * abs(float(J0[0]))
+    assert float((g1 - g0).abs().max() / g0.abs().max()) < 1e-11
