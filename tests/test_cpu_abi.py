@@ -114,3 +114,38 @@ def test_program_checks_reject_malformed_dct_ops():
     for P in (prog(fft_n=0), prog(fft_n=1), prog(nthreads=1024), prog(b=2, nslots=1)):
         assert L.pgx_run(ctypes.byref(P), ctypes.byref(inst), None) == 1   # PGX_E_ARG
     assert _lib.MAX_THREADS == 1024 and _lib.MAX_THREADS_FFT == 768
+
+
+@pytest.mark.parametrize("shape", [(33, 33), (65, 129), (129, 129), (513, 257), (1025, 65)])
+def test_tile_candidates_fit_the_launch_limits(shape):
+    """Every tile the autotuner may try (and the default pick), for every forward / reverse-mode
+    program form, fits the batched launch's shared memory (program + instance descriptor, the
+    check pgx_run_batched makes) and the thread limit of the kernel build it runs on."""
+    import ctypes
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import (L_ND, _candidates, _pick, build_programs, instance_params, launch_ops,
+                                          program_maxlen)
+    from pypde_gb300.navier.fused_adjoint import build_adjoint_programs
+    N, M = shape
+    lens, _ = instance_params(N, M, True, 0.01, 1e-3, 1e-3, (0.5, 0.5))
+    progs = (build_programs("CD", True) + build_programs("CN", True, rk3=True, split=True, beta=True) +
+             build_adjoint_programs("CD", True) + build_adjoint_programs("CN", True, split=True, beta=True, rk3=True))
+    limit = 227 * 1024
+    desc = -(-ctypes.sizeof(_lib.PgxInstance) // 16) * 16
+    for prog in progs:
+        lcap = (program_maxlen(prog, lens) + 1) | 1
+        fft_n = lens[L_ND + prog.axis] if prog.has_dct else 0
+        lines = lens[prog.lines]
+        tiles = _candidates(prog, lines * len(prog.variants), lcap, fft_n, lines)
+        tiles.append(_pick(prog, lines * len(prog.variants), lcap, fft_n, lines))
+        for tb, nt, wc, sd, dm in tiles:
+            ops = launch_ops(prog, sd, dm)
+            P = _lib.PgxProgram()
+            P.axis, P.lines_len, P.tb, P.lcap = prog.axis, 0, tb, lcap
+            P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), 0 if dm else fft_n, nt
+            for i, o in enumerate(ops):
+                P.ops[i] = o
+            smem = _lib.smem_bytes(P)
+            assert smem + desc + 1024 <= limit, (prog.name, shape, tb, nt, sd, dm, smem)
+            has_dct = any(o.code == _lib.OP["DCT"] for o in ops)
+            assert nt % 32 == 0 and nt <= (_lib.MAX_THREADS_FFT if has_dct else _lib.MAX_THREADS), (prog.name, nt)
