@@ -290,6 +290,8 @@ def run_gpu(args, rank, world):
         group_times = None
     else:  # instance groups as parallel branches of the step's graph: tuned like the tiles
         group_times = {str(k): round(v, 4) for k, v in fb.tune_groups().items()}
+        if not args.no_graph_tiles:   # the dominant pass's tiles once more, inside the step's graph
+            group_times["in_graph"] = {k: [list(v[0]), v[1]] for k, v in fb.tune_in_graph().items()}
     state_bytes = fb.state_arena.numel() * 8
     work_bytes = fb.scratch_bytes()
     flush, l2_note = l2_flusher(work_bytes)
@@ -680,6 +682,7 @@ def main():
     ap.add_argument("--adjoint-groups", type=int, default=1,
                     help="instance groups of the batched gradient, each on its own stream (measured on the "
                          "32-instance batch: 1 group 22.5, 4 groups 20.5, 8 groups 17.0 gradients/s)")
+    ap.add_argument("--no-graph-tiles", action="store_true", help="skip the in-graph second look at P2's tiles")
     ap.add_argument("--graph-groups", type=int, default=0,
                     help="instance groups as parallel branches of the step's graph (0: tuned, -K: K "
                          "per instance shape)")

@@ -1125,13 +1125,15 @@ class FusedBatch:
         The caller saves and restores whatever state the launches modify.  Graphs recorded over
         the old launches (here or by a HorizonGradient) see the new ``launch_generation``."""
         self.launch_generation = getattr(self, "launch_generation", 0) + 1
+        if not hasattr(self, "tune_log"):
+            self.tune_log = {}
         stream = torch.cuda.current_stream()
         chosen = {}
         for group in launch_sets:
             for gi, L0 in enumerate(group):
                 prog, key, members = L0["prog"], L0["key"], L0["members"]
                 lines = [self.insts[k].lines(prog) for k in members]
-                best = None
+                best, tried = None, []
                 for tb, nt, wc, sd, dm in _candidates(prog, sum(lines) * len(prog.variants), key[0], key[1],
                                                       max(lines)):
                     L = self._group_launch(prog, L0["d_insts"], key, members, tb, nt, wc, L0["name"], sd, dm)
@@ -1145,11 +1147,59 @@ class FusedBatch:
                     ms = a.elapsed_time(b) / reps
                     if verbose:
                         print(prog.name, gi, tb, nt, wc, sd, dm, round(ms, 4))
+                    tried.append((ms, (tb, nt, wc, sd, dm)))
                     if best is None or ms < best[0]:
                         best = (ms, L, tb, nt, wc, sd, dm)
                 group[gi] = best[1]
                 chosen["%s#%d" % (L0["name"], gi)] = best[2:] + (round(best[0], 4),)
+                self.tune_log["%s#%d" % (L0["name"], gi)] = sorted(tried)
         return chosen
+
+    def tune_in_graph(self, names=("P2",), within=0.15, reps=20, most=6):
+        """Second look at the tiles of the passes ``names`` inside the step's graph: the candidates
+        within ``within`` of a launch's best time alone are timed as part of the whole step (with
+        its parallel branches, as captured last), where other branches share the SMs; the fastest
+        step keeps its tile.  The state is restored after every trial.  Returns {tag: (tile, ms)}."""
+        groups = getattr(self, "graph_groups_arg", 1)
+        saved = self.state_arena.clone()
+
+        def step_ms():
+            self.capture(1, groups=groups)
+            for _ in range(3):
+                self.step()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for a, b in ev:
+                a.record()
+                self.step()
+                b.record()
+            torch.cuda.synchronize()
+            self.state_arena.copy_(saved)
+            return sum(a.elapsed_time(b) for a, b in ev) / reps
+
+        base = step_ms()
+        out = {}
+        for group in self.launches:
+            for gi, L0 in enumerate(group):
+                if L0["name"] not in names:
+                    continue
+                tag = "%s#%d" % (L0["name"], gi)
+                log = self.tune_log.get(tag, [])
+                cur = (L0["P"].tb, L0["P"].nthreads, L0["wc"], L0["sd"], L0["dm"])
+                cands = [t for ms, t in log if log and ms <= log[0][0] * (1.0 + within) and t != cur][:most]
+                best, best_ms = L0, base
+                for tb, nt, wc, sd, dm in cands:
+                    group[gi] = self._group_launch(L0["prog"], L0["d_insts"], L0["key"], L0["members"], tb, nt,
+                                                   wc, L0["name"], sd, dm)
+                    ms = step_ms()
+                    if ms < best_ms:
+                        best, best_ms = group[gi], ms
+                group[gi] = best
+                base = best_ms
+                out[tag] = ((best["P"].tb, best["P"].nthreads, best["wc"], best["sd"], best["dm"]), round(best_ms, 4))
+        self.launch_generation = getattr(self, "launch_generation", 0) + 1
+        self.capture(1, groups=groups)
+        torch.cuda.synchronize()
+        return out
 
     def autotune(self, reps=3, verbose=False):
         """Time every candidate tile shape of every launch of every pass on this batch and keep
@@ -1214,7 +1264,7 @@ class FusedBatch:
         for I, s in zip(self.insts, saved):
             for k, v in s.items():
                 I.arrays[k].copy_(v)
-        self.graph, self.graph_steps = g, nsteps
+        self.graph, self.graph_steps, self.graph_groups_arg = g, nsteps, groups
         # the graph reads the branches' instance descriptors and work lists: they live as long as it
         self.graph_branches = branches
         self.graph_groups = max(1, len(branches))
