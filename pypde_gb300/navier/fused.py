@@ -157,7 +157,7 @@ class Prog:
 
 
 def _split_convection_programs(tkind, fft, rk3, beta=False):
-    """P1, P2u, P2, P3, P3r with P1 / P2 / P3 written once for a generic field F (variants)."""
+    """P1, P2u, P2, P3, P3rs with P1 / P2 / P3 written once for a generic field F (variants)."""
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
     P = []
@@ -307,13 +307,13 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
     the previous stage's (UXO, UZO).
 
     ``split``: P1 - P3 as per-field programs run as three descriptors of one launch
-    (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3r (the non-convective
+    (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3rs (the non-convective
     right-hand-side terms, with the x-sweeps: P3rs): the same transforms in eleven passes, with three times
     the CTAs in the transform-heavy ones - for batches of few instances.
 
     ``beta``: diffusion beta-implicit (beta != 1, rbc2d.py:268-283, 390-391): the ADI tables and the
     pressure update carry beta (per-instance tables and parameters), and an extra pass P2e with
-    additions to P3 (P3r in the per-field form) put the explicit part into the right-hand sides."""
+    additions to P3 (P3rs in the per-field form) put the explicit part into the right-hand sides."""
     P = []
     BWD, FWD = _lib.DCT_BWD, _lib.DCT_FWD
     kinds = {"U": "CD", "V": "CD", "T": tkind}
@@ -321,7 +321,7 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
     if split:
         P += _split_convection_programs(tkind, fft, rk3, beta)
         if beta:
-            P.insert(3, _explicit_diffusion_y())   # P1, P2u, P2, P2e, P3, P3r
+            P.insert(3, _explicit_diffusion_y())   # P1, P2u, P2, P2e, P3, P3rs
     else:
         # P1 (x, lines M-2): physical-in-x parts of F and dF/dx
         p = Prog("P1", 0, L_MG, 2)

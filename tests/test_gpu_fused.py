@@ -264,7 +264,7 @@ BETA_CASES = [
                          ids=[f"{c[0]}-{c[1][0]}x{c[1][1]}-{c[2]['integrator']}-{c[3]}" for c in BETA_CASES])
 def test_fused_beta_vs_oracle(NS, case, shape, cfg, split):
     """beta != 1 (rbc2d.py:268-283, 390-391): beta-implicit ADI tables and pressure update, the explicit
-    diffusion through pass P2e and P3 / P3r; fused and per-field forms against the oracle."""
+    diffusion through pass P2e and P3 / P3rs; fused and per-field forms against the oracle."""
     from pypde_gb300.navier.fused import FusedBatch
     ns = NS(case=case, shape=shape, pr=1.0, tsave=None, **cfg)
     ns.set_temperature_noise(9, 1e-2)
