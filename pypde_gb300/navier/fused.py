@@ -308,8 +308,8 @@ def build_programs(tkind, fft, rk3=False, split=False, beta=False):
 
     ``split``: P1 - P3 as per-field programs run as three descriptors of one launch
     (U, V, T), plus P2u (velocities, D_y pres, S_y T) and P3rs (the non-convective
-    right-hand-side terms, with the x-sweeps: P3rs): the same transforms in eleven passes, with three times
-    the CTAs in the transform-heavy ones - for batches of few instances.
+    right-hand-side terms and the ADI x-sweeps): the same transforms in twelve passes, with three
+    times the CTAs in the transform-heavy ones - for batches of few instances.
 
     ``beta``: diffusion beta-implicit (beta != 1, rbc2d.py:268-283, 390-391): the ADI tables and the
     pressure update carry beta (per-instance tables and parameters), and an extra pass P2e with
