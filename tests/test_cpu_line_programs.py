@@ -346,3 +346,35 @@ def test_rk3_adjoint_is_the_transposed_step(tk):
             st[k].run(p)
     rhs = sum(float((arrays["b" + k] * d[k]).sum()) for k in STATE)
     assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)
+
+
+@pytest.mark.parametrize("beta", [1.0, 0.5])
+def test_rk3_step_split_matches_fused(beta):
+    """All three RK3 stages (velocities carried between stages through UXC / UXO): the per-field form
+    computes the fused form's step."""
+    st, arrays, rng = _rk3_machines(12, 13, "CN", 8)
+    if beta != 1.0:   # the beta parameters and the explicit-diffusion scratch
+        from pypde_gb300.navier.fused import P_EDT, P_EDU, P_MNU, scratch_shapes
+        for k, shp in scratch_shapes(12, 13, st[0].lens[5], st[0].lens[6], True).items():
+            arrays.setdefault(k, np.zeros(shp))
+        for m in st:
+            m.par = list(m.par)
+            m.par[P_EDU], m.par[P_EDT] = m.par[3] * (1 - beta) * 0.01, m.par[4] * (1 - beta)
+            m.par[P_MNU] *= beta
+            for k in scratch_shapes(12, 13, st[0].lens[5], st[0].lens[6], True):
+                m.arrays[k] = arrays[k]
+    keys = STATE + ("PG",)
+    X = {k: 1e-1 * rng.standard_normal(arrays[k].shape) for k in keys}
+    out = []
+    for split in (False, True):
+        for k in keys:
+            arrays[k][...] = X[k]
+        for k in ("UX_A", "UX_B", "UZ_A", "UZ_B"):
+            arrays[k][...] = 0.0
+        progs = build_programs("CN", True, rk3=True, split=split, beta=beta != 1.0)
+        for m in st:
+            for p in progs:
+                m.run(p)
+        out.append({k: arrays[k].copy() for k in STATE})
+    for k in STATE:
+        assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * np.abs(out[0][k]).max(), k
