@@ -106,6 +106,14 @@ def _oracle_steps(steps):
     return time.perf_counter() - t0, len(sols) * steps
 
 
+def _oracle_flavour():
+    """How the CPU oracle runs here: with its compiled banded sweeps (oracle/kernels.c, the
+    counterpart of the reference's Fortran) when built, else NumPy loops throughout."""
+    sys.path.insert(0, ROOT)
+    from oracle import _ck
+    return "NumPy restatement of the reference path" + (", banded sweeps in compiled C" if _ck.lib() else "")
+
+
 class CpuPort:
     """The CPU oracle (NumPy restatement of the reference path) on ``cores`` spawned
     processes, each owning a slice of the instances; solvers are built once."""
@@ -265,9 +273,9 @@ def run_gpu(args, rank, world):
             done, wall, steps_cpu = done + d, wall + w, steps_cpu + 1
         port.close()
         cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port",
-               "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (NumPy "
-                         "restatement of the reference path) in %d single-threaded processes, %.1f s of stepping"
-                         % (len(sample), len(specs), steps_cpu, ncores, wall)}
+               "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (%s) "
+                         "in %d single-threaded processes, %.1f s of stepping"
+                         % (len(sample), len(specs), steps_cpu, _oracle_flavour(), ncores, wall)}
 
     solvers, fb = build_batch(specs, {"auto": None, "on": True, "off": False}[args.split])
     n_inst = len(solvers)
@@ -660,9 +668,9 @@ def run_reference(args, rank, world):
             "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=full), "instances_per_gpu": full},
             "cpu_baseline": {"value": round(value, 3), "unit": "instance-steps/s", "cores": cores, "kind": "port",
                              "sample": "every %s instance (%d of %d, same size / Ra mix), 1 step per timed step, "
-                                       "%d single-threaded spawned processes running the CPU oracle (NumPy "
-                                       "restatement of the reference path)" % ("4th" if full != len(specs) else
-                                                                               "", len(specs), full, cores)},
+                                       "%d single-threaded spawned processes running the CPU oracle (%s)"
+                                       % ("4th" if full != len(specs) else "", len(specs), full, cores,
+                                          _oracle_flavour())},
             "e2e": {"value": round(value, 3), "unit": "instance-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 

@@ -18,6 +18,9 @@ spectral  DCT-I, Chebyshev / Shen bases, stencils, derivative recurrence
 linalg    TDMA (offset k), FDMA, TwoDMA, FDMA type-2 (Poisson) sweeps
 field     2-D transforms with 3/2 dealiasing, grad, convective term, averages
 solver    ADI Helmholtz and fast-diagonalised Poisson plans
+kernels.c the banded sweeps and the derivative recurrence in C (same operations,
+          same order, no FMA contraction: bit-equal to the NumPy loops), loaded
+          by _ck when built; without it the NumPy loops run
 rbc2d     Rayleigh-Benard IMEX step, Nusselt numbers, kinetic energy
 """
 from . import spectral, linalg, field, solver, rbc2d  # noqa: F401

@@ -7,6 +7,8 @@ Fortran whole-row array statements are.  0-based indices throughout.
 """
 import numpy as np
 
+from . import _ck
+
 
 def tdma_offset(a, b, c, d, k):
     """solve_tdma_2d (tdma.f90:56-107): A x = d, A banded at offsets -k, 0, +k.
@@ -15,6 +17,14 @@ def tdma_offset(a, b, c, d, k):
     """
     d = np.asarray(d, dtype=np.float64)
     n = b.shape[0]
+    L = _ck.lib()
+    if L is not None and n > k:
+        dd = _ck.c64(d.reshape(n, -1))
+        m = dd.shape[1]
+        g, x, w = np.empty_like(dd), np.empty_like(dd), np.zeros(n - k)
+        a, b, c = _ck.c64(a), _ck.c64(b), _ck.c64(c)
+        L.ok_tdma_offset(_ck.ptr(a), _ck.ptr(b), _ck.ptr(c), _ck.ptr(dd), _ck.ptr(x), _ck.ptr(g), _ck.ptr(w), n, m, k)
+        return x.reshape(d.shape)
     w = np.zeros(n - k)
     for i in range(n - k):
         w[i] = c[i] / b[i] if i < k else c[i] / (b[i] - a[i - k] * w[i - k])
@@ -34,6 +44,11 @@ def tdma_offset(a, b, c, d, k):
 def fdma_lu(l, d, u1, u2):
     """Plan_fdma.FDMA_LU (plans.py:226-234) == init_fdma's sweep (fdma.f90:135-141), in place."""
     n = d.shape[0]
+    L = _ck.lib()
+    if L is not None and d.ndim == 2 and n >= 4 and all(v.flags.c_contiguous and v.dtype == np.float64
+                                                         for v in (l, d, u1, u2)):
+        L.ok_fdma_lu(_ck.ptr(l), _ck.ptr(d), _ck.ptr(u1), _ck.ptr(u2), n, d.shape[1])
+        return l, d, u1, u2
     for i in range(2, n):
         l[i - 2] = l[i - 2] / d[i - 2]
         d[i] = d[i] - l[i - 2] * u1[i - 2]
@@ -54,6 +69,17 @@ def fdma_factor(A):
 def fdma_solve(l, d, u1, u2, x):
     """solve_fdma_1d / solve_fdma_2d along axis 0 (fdma.f90:1-38, 68-81), in place on x."""
     n = d.shape[0]
+    L = _ck.lib()
+    if L is not None and n >= 4:
+        cs = 1 if d.ndim == 2 else 0
+        xx = _ck.c64(x.reshape(n, -1))
+        m = xx.shape[1]
+        if not cs or d.shape[1] == m:
+            co = [_ck.c64(v) for v in (l, d, u1, u2)]
+            L.ok_fdma_solve(*[_ck.ptr(v) for v in co], cs, _ck.ptr(xx), n, m)
+            if not np.shares_memory(xx, x):
+                x[...] = xx.reshape(x.shape)
+            return x
     for i in range(2, n):
         x[i] -= l[i - 2] * x[i - 2]
     x[n - 1] = x[n - 1] / d[n - 1]
@@ -75,6 +101,14 @@ def fdma_solve_axis(l, d, u1, u2, x, axis):
 def twodma_solve(d, u, x):
     """solve_twodma_1d / _2d along axis 0 (twodma.f90:2-62), in place on x."""
     n = d.shape[0]
+    L = _ck.lib()
+    if L is not None and n >= 2:
+        xx = _ck.c64(x.reshape(n, -1))
+        d, u = _ck.c64(d), _ck.c64(u)
+        L.ok_twodma_solve(_ck.ptr(d), _ck.ptr(u), _ck.ptr(xx), n, xx.shape[1])
+        if not np.shares_memory(xx, x):
+            x[...] = xx.reshape(x.shape)
+        return x
     x[n - 1] = x[n - 1] / d[n - 1]
     x[n - 2] = x[n - 2] / d[n - 2]
     for i in range(n - 3, -1, -1):
@@ -85,12 +119,9 @@ def twodma_solve(d, u, x):
 def _band4(A):
     """Diagonals d, l(-2), u1(+2), u2(+4) of a square (stack of) matrices, zero-padded
     to full length like init_fdma's zero initialisation (fdma.f90:124-133)."""
-    n = A.shape[-1]
-    d = np.array([A[..., i, i] for i in range(n)])
-    l = np.array([A[..., i, i - 2] for i in range(2, n)])
-    u1 = np.array([A[..., i, i + 2] for i in range(n - 2)])
-    u2 = np.array([A[..., i, i + 4] for i in range(n - 4)])
-    return l, d, u1, u2
+    def diag(k):  # rows first: (n - |k|, ...) C-contiguous
+        return np.ascontiguousarray(np.moveaxis(np.diagonal(A, k, -2, -1), -1, 0))
+    return diag(-2), diag(0), diag(2), diag(4)
 
 
 def fdma_type2(A, C, lam, x, singular):

@@ -7,6 +7,8 @@ All arrays are float64; 1-D operations act along ``axis`` of an N-D array.
 import numpy as np
 import scipy.fft
 
+from . import _ck
+
 from . import linalg
 
 # Basis keys as accepted by pypde's Base() factory (spectralbase.py:25-45).
@@ -182,6 +184,12 @@ def cheb_diff1(c, axis=0):
     """
     c = np.moveaxis(np.asarray(c, dtype=np.float64), axis, 0)
     n = c.shape[0]
+    L = _ck.lib()
+    if L is not None and n >= 3:
+        cc = _ck.c64(c.reshape(n, -1))
+        dc = np.zeros_like(cc)
+        L.ok_cheb_diff1(_ck.ptr(cc), _ck.ptr(dc), n, cc.shape[1])
+        return np.moveaxis(dc.reshape(c.shape), 0, axis)
     dc = np.zeros_like(c)
     dc[n - 2] = 2.0 * (n - 1) * c[n - 1]
     for j in range(n - 3, 0, -1):
