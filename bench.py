@@ -272,7 +272,7 @@ def run_gpu(args, rank, world):
             d, w = port.step(1)
             done, wall, steps_cpu = done + d, wall + w, steps_cpu + 1
         port.close()
-        cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port",
+        cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port", "blas_threads": 1,
                "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (%s) "
                          "in %d single-threaded processes, %.1f s of stepping"
                          % (len(sample), len(specs), steps_cpu, _oracle_flavour(), ncores, wall)}
@@ -667,6 +667,7 @@ def run_reference(args, rank, world):
             "data": "synthetic: seeded U(-1,1) temperature noise (seeds 100+i)", "impl": "reference",
             "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=full), "instances_per_gpu": full},
             "cpu_baseline": {"value": round(value, 3), "unit": "instance-steps/s", "cores": cores, "kind": "port",
+                             "blas_threads": 1,
                              "sample": "every %s instance (%d of %d, same size / Ra mix), 1 step per timed step, "
                                        "%d single-threaded spawned processes running the CPU oracle (%s)"
                                        % ("4th" if full != len(specs) else "", len(specs), full, cores,
