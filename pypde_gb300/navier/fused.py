@@ -1183,7 +1183,7 @@ class FusedBatch:
                 if L0["name"] not in names:
                     continue
                 tag = "%s#%d" % (L0["name"], gi)
-                log = self.tune_log.get(tag, [])
+                log = getattr(self, "tune_log", {}).get(tag, [])
                 cur = (L0["P"].tb, L0["P"].nthreads, L0["wc"], L0["sd"], L0["dm"])
                 cands = [t for ms, t in log if log and ms <= log[0][0] * (1.0 + within) and t != cur][:most]
                 best, best_ms = L0, base
@@ -1343,17 +1343,22 @@ class FusedBatch:
         self._pipe_fresh = True
         return len(self._pipe)
 
-    def step_host(self, host):
+    def step_host(self, host, wait=False):
         """One step of every instance with the state in host memory: ``host`` (pinned, the layout of
         ``state_arena``) is copied in, stepped and copied back.  The instance groups of
         ``host_pipeline`` run on their own streams, so one group's copies overlap another's
         passes and the next step's upload of a group follows its own download; the current
-        stream waits for all groups before the call returns (asynchronously)."""
+        stream waits for all groups before the call returns (asynchronously).
+
+        Between two calls the groups do not wait for the current stream, so that consecutive
+        steps overlap.  Work enqueued on the current stream since the last call that reads or
+        writes ``host`` or ``state_arena`` needs ``wait=True`` (the groups then start after it;
+        the first call always does)."""
         if getattr(self, "_pipe", None) is None:
             self.host_pipeline()
         main = torch.cuda.current_stream()
         for sub, o0, o1, st in self._pipe:
-            if self._pipe_fresh:
+            if self._pipe_fresh or wait:
                 st.wait_stream(main)
             with torch.cuda.stream(st):
                 self.state_arena[o0:o1].copy_(host[o0:o1], non_blocking=True)

@@ -238,8 +238,8 @@ def test_step_host_pipeline_matches_step(NS):
             assert fb.host_pipeline(3) >= 2
             host = torch.empty(fb.state_arena.numel(), dtype=torch.float64, pin_memory=True)
             host.copy_(fb.state_arena)
-            for _ in range(4):
-                fb.step_host(host)
+            for i in range(4):
+                fb.step_host(host, wait=i == 2)
             torch.cuda.synchronize()
             runs.append(host.clone())
         else:
