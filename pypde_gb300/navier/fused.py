@@ -1402,7 +1402,7 @@ def _log2(x):
 def program_work(prog, I):
     """Algorithmic work of ``prog`` on instance ``I``: (flops, bytes).
 
-    Counts per line of n elements: DCT-I 2.5 n log2(2(n-1)) (the FFT count);
+    Counts per line of n elements: DCT-I 2.5 n log2(2(n-1)) (the FFT count) per slot;
     stencil / transpose 2 per output; derivative 2 per element and pass;
     offset-2 TDMA 5; four-diagonal sweep 7; Poisson sweep 9; banded 2 per
     diagonal and row; dense 2 per column and row; scale / mul 1, axpy /
@@ -1440,9 +1440,9 @@ def program_work(prog, I):
             fl += 5.0 * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
         elif code in (_lib.OP["DIFF"], _lib.OP["DIFF_T"]):
             fl += 2.0 * o.k * sum(slen[o.a:o.a + max(o.b, 1)]) * lines
-        elif code == _lib.OP["DCT"]:
+        elif code == _lib.OP["DCT"]:   # every slot of a multi-slot op is one transform
             n = slen[o.a]
-            fl += 2.5 * n * _log2(2 * (n - 1)) * lines
+            fl += 2.5 * n * _log2(2 * (n - 1)) * lines * max(o.b, 1)
         elif code == _lib.OP["BANDED"]:
             slen[o.a] = I.lens[o.len]
             fl += 2.0 * o.k * slen[o.a] * lines

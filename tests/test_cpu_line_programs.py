@@ -378,3 +378,27 @@ def test_rk3_step_split_matches_fused(beta):
         out.append({k: arrays[k].copy() for k in STATE})
     for k in STATE:
         assert np.abs(out[1][k] - out[0][k]).max() <= 1e-12 * np.abs(out[0][k]).max(), k
+
+
+@pytest.mark.parametrize("rk3", [False, True])
+@pytest.mark.parametrize("beta", [False, True])
+def test_algorithmic_work_of_both_forms_agrees(rk3, beta):
+    """The roofline's algorithmic flop count: the fused and the per-field form of the step do the same
+    transforms (a multi-slot DCT op counts one transform per slot), so their totals agree to the few
+    extra pointwise operations of the per-field form."""
+    import types
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import Prog, program_work
+    lens, _ = instance_params(65, 33, True, 0.01, 1e-3, 1e-3, (0.5, 0.5))
+    inst = types.SimpleNamespace(lens=lens)
+    tot = []
+    for split in (False, True):
+        progs = build_programs("CD", True, rk3=rk3, split=split, beta=beta)
+        tot.append(sum(program_work(p, inst)[0] * len(p.variants) for p in progs))
+    assert abs(tot[1] - tot[0]) <= 0.02 * tot[0], tot
+    one, three = Prog("a", 1, 6, 4), Prog("b", 1, 6, 4)
+    for p, count in ((one, 1), (three, 3)):
+        for s in range(count):
+            p.load(s, "X", 6)
+        p.dct(0, _lib.DCT_FWD, True, count=count)
+    assert program_work(three, inst)[0] == pytest.approx(3 * program_work(one, inst)[0])
