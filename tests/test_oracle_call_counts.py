@@ -4,7 +4,8 @@
 reference itself) lists, for one Rayleigh-Benard step of six configurations, every call of
 the reference's native kernels -- scipy's DCT-I and the f2py modules differentiate_cheby,
 tdma, twodma, fdma -- by family, transform length and number of lines.  The oracle's
-counterparts are counted on the same step here and must match call for call.
+counterparts are counted on the same step here and must match call for call.  The fused step's programs are held
+to the same counts: the same transform lengths and never more line transforms.
 """
 import collections
 import json
@@ -66,3 +67,46 @@ def test_oracle_kernel_calls_match_reference(counted, tag):
     ns.update()
     got = sorted([list(k) + [v] for k, v in counted.items()])
     assert got == calls
+
+
+def _fused_dct_lines(tag):
+    """{transform length: line transforms} of the fused step's programs for the configuration ``tag``."""
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import build_programs, instance_params
+    cfg = CASES[tag]
+    N, M = cfg["shape"]
+    lens, _ = instance_params(N, M, cfg.get("dealias", True), 0.01, 1e-3, 1e-3, (0.5, 0.5))
+    rk3 = cfg.get("integrator") == "rk3"
+    progs = build_programs("CN" if cfg["case"] == "rbc" else "CD", True, rk3=rk3, split=False,
+                           beta=cfg.get("beta", 1.0) != 1.0)
+    op = _lib.OP
+    got = collections.Counter()
+    for p in progs * (3 if rk3 else 1):
+        slen = [0] * 8
+        for o in p.ops:
+            if o.code in (op["LOAD"], op["SETLEN"], op["BANDED"], op["DENSE"]):
+                slen[o.a] = lens[o.len]
+            elif o.code == op["COPY"]:
+                slen[o.a] = slen[o.b]
+            elif o.code in (op["AXPY"], op["MUL"]):
+                slen[o.a] = max(slen[o.a], slen[o.b])
+            elif o.code in (op["STENCIL"], op["STENCIL_T"]):
+                slen[o.a] += 2 if o.code == op["STENCIL"] else -2
+            elif o.code == op["DCT"]:
+                got[slen[o.a]] += lens[p.lines] * max(o.b, 1) * len(p.variants)
+    return got
+
+
+@pytest.mark.parametrize("tag", sorted(CASES))
+def test_fused_step_transforms_no_more_lines_than_the_reference(tag):
+    """The fused step's DCT-I line transforms, by length, against the reference's (same lengths,
+    never more lines: the fused passes skip the zero-padded lines of the 3/2 grid and RK3 reuses
+    the previous stage's velocities)."""
+    ref = collections.Counter()
+    for fam, n, lines, k in CASES[tag]["calls"]:
+        if fam == "dct":
+            ref[n] += lines * k
+    got = _fused_dct_lines(tag)
+    assert set(got) == set(ref)
+    for n in ref:
+        assert 0.55 * ref[n] <= got[n] <= ref[n], (n, got[n], ref[n])
