@@ -135,8 +135,17 @@ int64_t pgx_program_smem(const pgx_program* prog);
  * the kernel by value. */
 int pgx_run(const pgx_program* prog, const pgx_instance* inst, void* stream);
 
+/* The checks pgx_run applies to a program and an instance descriptor (both
+ * HOST memory), without a launch and without a device: array extents and
+ * lengths within the slot capacity, the tables the ops read present.  Returns
+ * PGX_OK or PGX_E_ARG.  The shared-memory capacity is checked at launch. */
+int pgx_check_instance(const pgx_program* prog, const pgx_instance* inst);
+
 /* Run one pass over many instances.  `d_insts` (ninst entries) and `d_work`
- * (nwork (instance, tile) int32 pairs) are DEVICE memory. */
+ * (nwork (instance, tile) int32 pairs) are DEVICE memory, which this call does
+ * not read: every descriptor must pass pgx_check_instance (on its host copy,
+ * before the upload) and every work pair must name an entry of `d_insts` and a
+ * tile below ceil(lines / prog->tb) of it. */
 int pgx_run_batched(const pgx_program* prog, const pgx_instance* d_insts,
                     const int32_t* d_work, int32_t nwork, void* stream);
 

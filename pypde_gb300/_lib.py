@@ -55,6 +55,7 @@ SIGNATURES = {
     "pgx_version": (ctypes.c_int, []),
     "pgx_program_smem": (ctypes.c_int64, [ctypes.c_void_p]),
     "pgx_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pgx_check_instance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pgx_run_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                        ctypes.c_void_p]),
     "pgx_dct1": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32,

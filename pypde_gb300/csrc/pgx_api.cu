@@ -64,7 +64,9 @@ static int smem_optin_max() {
 // its DFMA rate).
 static const int DENSE_MMA_MAX_N = 33;
 
-static int check_program(const pgx_program* P) {
+// The program's own consistency (limits, slots, indices); the shared-memory capacity is checked
+// against the device by check_program.
+static int check_program_shape(const pgx_program* P) {
   if (!P) return PGX_E_ARG;
   if (P->axis < 0 || P->axis > 1 || P->tb < 1 || P->lcap < 1 || P->lcap > PGX_LMAX + 8) return PGX_E_ARG;
   if (P->nslots < 1 || P->nslots > PGX_MAX_SLOTS || P->nops < 0 || P->nops > PGX_MAX_OPS) return PGX_E_ARG;
@@ -87,6 +89,12 @@ static int check_program(const pgx_program* P) {
       return PGX_E_ARG;
     if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;
   }
+  return PGX_OK;
+}
+
+static int check_program(const pgx_program* P) {
+  int rc = check_program_shape(P);
+  if (rc) return rc;
   int64_t need = pgx_program_smem(P) + 1024;
   if (need > smem_optin_max()) return PGX_E_SMEM;
   return PGX_OK;
@@ -147,6 +155,13 @@ extern "C" int pgx_run(const pgx_program* P, const pgx_instance* I, void* stream
   int e = pgx::launch_single(P, I, (cudaStream_t)stream, ntiles);
   if (e) return cuda_fail((cudaError_t)e);
   return PGX_OK;
+}
+
+extern "C" int pgx_check_instance(const pgx_program* P, const pgx_instance* I) {
+  int rc = check_program_shape(P);
+  if (rc) return rc;
+  if (!I || P->lines_len < 0) return PGX_E_ARG;
+  return check_instance(P, I);
 }
 
 extern "C" int pgx_run_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work,
