@@ -116,6 +116,34 @@ def test_program_checks_reject_malformed_dct_ops():
     assert _lib.MAX_THREADS == 1024 and _lib.MAX_THREADS_FFT == 768
 
 
+def test_instance_checks_on_host_descriptors():
+    """pgx_check_instance (no device needed) accepts a consistent descriptor and refuses one whose
+    array is longer than the slot capacity, whose length exceeds it, or whose table is missing."""
+    from pypde_gb300 import _lib
+    L = _lib.lib()
+    P = _lib.PgxProgram()
+    P.axis, P.lines_len, P.tb, P.lcap, P.nslots, P.fft_n, P.nthreads = 0, 1, 2, 11, 1, 9, 256
+    ops = [_lib.op("LOAD", a=0, arr=0, len=0), _lib.op("DCT", a=0, b=1, mat=0, k=_lib.DCT_FWD),
+           _lib.op("STORE", a=0, arr=1)]
+    P.nops = len(ops)
+    for i, o in enumerate(ops):
+        P.ops[i] = o
+
+    def inst(n0=9, length=9, table=4096):
+        I = _lib.PgxInstance()
+        for a in (0, 1):
+            I.arr[a].ptr, I.arr[a].s0, I.arr[a].s1, I.arr[a].n0, I.arr[a].n1 = 4096, 5, 1, n0, 5
+        I.len[0], I.len[1] = length, 5
+        I.mat[0] = table
+        return I
+
+    ok = inst()
+    assert L.pgx_check_instance(ctypes.byref(P), ctypes.byref(ok)) == 0
+    for bad in (inst(n0=12), inst(length=11), inst(table=0)):
+        assert L.pgx_check_instance(ctypes.byref(P), ctypes.byref(bad)) == 1     # PGX_E_ARG
+    assert L.pgx_check_instance(None, ctypes.byref(ok)) == 1
+
+
 @pytest.mark.parametrize("shape", [(33, 33), (65, 129), (129, 129), (513, 257), (1025, 65)])
 def test_tile_candidates_fit_the_launch_limits(shape):
     """Every tile the autotuner may try (and the default pick), for every forward / reverse-mode
