@@ -22,8 +22,14 @@ def build(force=False):
 
 
 def lib():
-    """The loaded library, or None when it is not built."""
+    """The loaded library, or None when it is not built (a build older than kernels.c is rebuilt
+    first, or left unused when that fails)."""
     global _lib
+    if _lib is None and os.path.exists(LIB) and os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        try:
+            build()
+        except Exception:  # no compiler: the NumPy loops run
+            return None
     if _lib is None and os.path.exists(LIB):
         L = ctypes.CDLL(LIB)
         P, I = ctypes.c_void_p, ctypes.c_int
