@@ -17,7 +17,9 @@ def build(force=False):
     """gcc -O2, no floating-point contraction (bit-equal to the NumPy loops); returns the path."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
-        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB, SRC], check=True)
+        tmp = "%s.%d.tmp" % (LIB, os.getpid())   # concurrent builders each write their own file
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, SRC], check=True)
+        os.replace(tmp, LIB)
     return LIB
 
 
