@@ -1055,8 +1055,9 @@ class FusedBatch:
             for v, var in enumerate(prog.variants):
                 I.fill(prog, insts[k * nv + v], stage, var)
         d = torch.frombuffer(bytearray(bytes(insts)), dtype=torch.uint8).to(device())
-        # host copies, by device address, for the launch checks of _group_launch
-        self.__dict__.setdefault("_host_insts", {})[d.data_ptr()] = insts
+        # the host copy travels with the device descriptors: _group_launch checks every
+        # launch against it (the batched kernel reads its descriptors on the device only)
+        d.pgx_host = insts
         return d
 
     def _group_launch(self, prog, d_insts, key, members, tb, nt, wc=False, name=None, sd=False, dm=False):
@@ -1077,13 +1078,15 @@ class FusedBatch:
                 P.ops[i].k = o.k | _lib.CHAIN_WARP
         nv = len(prog.variants)
         # the batched launch cannot read its descriptors on the host: check every member's host copy
-        host = getattr(self, "_host_insts", {}).get(d_insts.data_ptr())
-        if host is not None:
-            check = _lib.lib().pgx_check_instance
-            for k in members:
-                for v in range(nv):
-                    _lib.check(check(ctypes.byref(P), ctypes.byref(host[k * nv + v])),
-                               "%s: instance %d, variant %d" % (name or prog.name, k, v))
+        host = getattr(d_insts, "pgx_host", None)
+        if host is None:
+            raise RuntimeError("%s: launch descriptors without their host copy (not made by _d_insts)"
+                               % (name or prog.name))
+        check = _lib.lib().pgx_check_instance
+        for k in members:
+            for v in range(nv):
+                _lib.check(check(ctypes.byref(P), ctypes.byref(host[k * nv + v])),
+                           "%s: instance %d, variant %d" % (name or prog.name, k, v))
         work = [(k * nv + v, t) for k in members for v in range(nv)
                 for t in range(-(-self.insts[k].lines(prog) // tb))]
         d_work = torch.as_tensor(np.asarray(work, dtype=np.int32).ravel(), device=device())
@@ -1109,7 +1112,6 @@ class FusedBatch:
     def _build_launches(self, tiles=None):
         """Launch descriptors of the forward passes; ``tiles`` = {"pass#group": (lines per CTA,
         threads)} overrides the default choice (e.g. another batch's autotuned tiles)."""
-        self._host_insts = {}
         self.launches = [self._pass_launches(p, tiles, st) for st in range(self.nstage) for p in self.progs]
         # a graph recorded before reads the old launches' descriptors and work lists: drop it with them
         self.graph, self.graph_branches = None, []

@@ -1,7 +1,7 @@
 """Record which native kernels the pypde reference calls in one Rayleigh-Benard time step.
 
-Run from the repository root in a container that has the reference checked out
-(default /root/reference):
+Run from the repository root in a container that has the reference checked out,
+its location given by ``--reference`` or the PYPDE_REFERENCE variable:
 
     python tests/golden/make_call_counts.py [--reference PATH]
 

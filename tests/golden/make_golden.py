@@ -1,7 +1,7 @@
 """Generate golden vectors by running the unmodified pypde reference.
 
 Run from the repository root in a container that has the reference checked
-out (default /root/reference):
+out, its location given by ``--reference`` or the PYPDE_REFERENCE variable:
 
     python tests/golden/make_golden.py [--reference PATH]
 

@@ -17,13 +17,16 @@ tests, the benchmark or the product package.
   did and what its f2py calls rely on: the Poisson plan feeds eig's output to
   a ``real(8), intent(inout)`` Fortran argument (plans.py:310-314).
 """
+import os
 import sys
 import types
 import warnings
 
 import numpy as np
 
-REFERENCE = "/root/reference"
+# Where the pypde checkout lives: the PYPDE_REFERENCE environment variable, or the
+# --reference argument of the generating scripts.
+REFERENCE = os.environ.get("PYPDE_REFERENCE")
 
 
 def _f_inout(x, name):
@@ -195,6 +198,9 @@ def _module(name, **attrs):
 
 def install(reference=REFERENCE):
     """Register the shims and stubs, patch eig, and put the reference on sys.path."""
+    if not reference or not os.path.isdir(os.path.join(reference, "pypde")):
+        raise SystemExit("pypde reference checkout not found: pass --reference PATH or set PYPDE_REFERENCE "
+                         "(got %r)" % (reference,))
     anything = lambda *a, **k: None  # noqa: E731
     stub = _module("stub")
     for name in ["matplotlib", "matplotlib.pyplot", "matplotlib.animation", "mpl_toolkits",

@@ -136,3 +136,17 @@ def test_launch_descriptors_other_shapes(shapes, rk3):
             fb = stand_in_batch(shapes, dealias, "CN", True, rk3, False, split)
             progs = F.build_programs("CN", True, rk3=rk3, split=split)
             assert check_every_tile(fb, progs + FA.build_adjoint_programs("CN", True, split, rk3=rk3)) > 0
+
+
+def test_launch_without_host_descriptors_is_refused():
+    """Descriptors not made by _d_insts carry no host copy: building a launch over them raises
+    instead of skipping the instance checks."""
+    fb = stand_in_batch([(33, 33)], True, "CD", True, False, False, False)
+    prog = F.build_programs("CD", True)[0]
+    d = fb._d_insts(prog, 0)
+    bare = d.clone()  # same bytes, no host copy attached
+    (key, members), = fb._groups(prog)
+    tb, nt, wc, sd, dm = F._pick(prog, fb.insts[0].lines(prog), key[0], key[1], fb.insts[0].lines(prog))
+    fb._group_launch(prog, d, key, members, tb, nt, wc, prog.name, sd, dm)
+    with pytest.raises(RuntimeError, match="host copy"):
+        fb._group_launch(prog, bare, key, members, tb, nt, wc, prog.name, sd, dm)
