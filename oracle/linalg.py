@@ -139,14 +139,21 @@ def fdma_type2(A, C, lam, x, singular):
     if singular:
         sing = np.abs(lam) < 1e-10
     reg = ~sing
+    # the four diagonals of A + C*lam_i, element for element the Fortran's A(i,j) + C(i,j)*lam(i),
+    # formed from the diagonals of A and C (no dense matrix per eigenvalue)
+    bA, bC = _band4(A), _band4(C)
+
+    def band(lams, first):
+        return [np.ascontiguousarray(a[first:, None] + c[first:, None] * lams[None, :]) for a, c in zip(bA, bC)]
+
     if reg.any():
-        l, d, u1, u2 = _band4(A[None, :, :] + C[None, :, :] * lam[reg][:, None, None])
+        l, d, u1, u2 = band(lam[reg], 0)
         fdma_lu(l, d, u1, u2)
         xr = x[:, reg]
         fdma_solve(l, d, u1, u2, xr)
         x[:, reg] = xr
     if sing.any():
-        l, d, u1, u2 = _band4(A[None, 1:, 1:] + C[None, 1:, 1:] * lam[sing][:, None, None])
+        l, d, u1, u2 = band(lam[sing], 1)
         fdma_lu(l, d, u1, u2)
         xs = x[1:, sing]
         fdma_solve(l, d, u1, u2, xs)

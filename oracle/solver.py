@@ -97,3 +97,34 @@ class Poisson2D:
     def solve_lhs(self, b):
         x = linalg.fdma_type2(self.Ax, self.Cx, self.wy, b, singular=True)
         return apply_along(self.Qy, x, 1)
+
+
+class HholtzFD:
+    """(I - lam Laplacian) u = rhs + u_old by fast diagonalisation in y, exactly (no ADI splitting).
+
+    The reference's Plan_Poisson (plans.py:254-341, solve_fdma_type2 of fdma.f90:146-185) with
+    A = -lam/scale_x^2 I_x S_x, C = B_x S_x and alpha_i = 1 - lam w_i, where w, Q_y are the
+    eigenpairs of C_y^-1 I_y S_y / scale_y^2 that solverplan_poisson2d builds (poisson.py:43-110):
+    rhs plans B_x along x, H_y = Q_y^-1 C_y^-1 B_y along y; old plans C_x along x, Q_y^-1 along y;
+    lhs the per-eigenvalue type-2 sweep along x (no singular mode: alpha_i >= 1), then Q_y along y.
+    """
+
+    def __init__(self, keys, shape, lam, scale=(1.0, 1.0)):
+        po = Poisson2D(keys, shape, singular=False, scale=scale)
+        self.A = -lam * po.Ax
+        self.C = po.Cx
+        self.alpha = 1.0 - lam * po.wy
+        self.Bx, self.Hy, self.Qy = po.Bx, po.Hy, po.Qy
+        self.QyI = np.linalg.inv(po.Qy)
+
+    def solve_rhs(self, b):
+        b = apply_along(self.Bx, b, 0)
+        return apply_along(self.Hy, b, 1)
+
+    def solve_old(self, b):
+        b = apply_along(self.C, b, 0)
+        return apply_along(self.QyI, b, 1)
+
+    def solve_lhs(self, b):
+        x = linalg.fdma_type2(self.A, self.C, self.alpha, b, singular=False)
+        return apply_along(self.Qy, x, 1)

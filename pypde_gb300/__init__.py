@@ -12,7 +12,8 @@ from .field_operations import (grad, cheby_to_galerkin, galerkin_to_cheby, conv_
                                avg_vol, interpolate)
 from .solver import (Flags, MetaPlan, MatrixBase, PlanRHS, PlanLHS, Plan_numpy, Plan_twodma, Plan_fdma,
                      Plan_Poisson, SolverPlan, Integrator)
-from .templates import solverplan_hholtz1d, solverplan_hholtz2d_adi, solverplan_poisson1d, solverplan_poisson2d
+from .templates import (solverplan_hholtz1d, solverplan_hholtz2d_adi, solverplan_hholtz2d_fd, solverplan_poisson1d,
+                        solverplan_poisson2d)
 from ._lib import PgxError
 
 __version__ = "0.1.0"

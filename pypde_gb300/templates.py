@@ -44,6 +44,31 @@ def solverplan_hholtz2d_adi(bases, lam, scale=(1, 1)):
     return solver
 
 
+def solverplan_hholtz2d_fd(bases, lam, scale=(1, 1)):
+    """(I - lam Laplacian) u = rhs + u_old solved exactly by fast diagonalisation in y.
+
+    pypde has no template for this; it composes the reference's own pieces: the
+    eigendecomposition of solverplan_poisson2d (poisson.py:43-110) and its Plan_Poisson
+    (plans.py:254-341) with A = -lam/scale_x^2 I_x S_x, C = B_x S_x and alpha_i = 1 - lam w_i.
+    rhs: B_x along x, H_y = Q_y^-1 C_y^-1 B_y along y; old: C_x along x, Q_y^-1 along y;
+    lhs: the per-eigenvalue four-diagonal sweep along x (alpha_i >= 1, no singular mode), then
+    Q_y along y.  Unlike solverplan_hholtz2d_adi it does not split the operator, so its result
+    differs from the ADI plan's by the splitting error (lam^2 D_x^2 D_y^2 u)."""
+    field = Field(bases)
+    assert field.ndim == 2
+    fd = poisson2d_matrices(_axis_mats(field.xs[0]), _axis_mats(field.xs[1]), False, scale)
+    solver = SolverPlan()
+    solver.add_rhs(PlanRHS(fd["Bx"], ndim=2, axis=0))
+    solver.add_rhs(PlanRHS(fd["Hy"], ndim=2, axis=1))
+    solver.add_old(PlanRHS(fd["Cx"], ndim=2, axis=0))
+    solver.add_old(PlanRHS(np.linalg.inv(fd["Qy"]), ndim=2, axis=1))
+    solver.add_lhs(PlanLHS(-lam * fd["Ax"], alpha=1.0 - lam * np.real(fd["wy"]), C=fd["Cx"], ndim=2, axis=0,
+                           method="poisson", singular=False))
+    solver.add_lhs(PlanLHS(fd["Qy"], ndim=2, axis=1, method="multiply"))
+    solver._fd = fd
+    return solver
+
+
 def solverplan_poisson1d(bases, singular=False):
     """D2 u = rhs premultiplied by B (poisson.py:4-40)."""
     field = Field(bases)
