@@ -1,4 +1,4 @@
-"""Steady states of the Rayleigh-Benard step by Newton-Krylov on the GPU (navier/rbc2d_base.py:260-341).
+"""Steady states of the Rayleigh-Benard step by Newton-Krylov (navier/rbc2d_base.py:260-341).
 
 pypde's ``NavierStokesSteadyState.solve_steady_state`` hands the residual
 
@@ -6,8 +6,15 @@ pypde's ``NavierStokesSteadyState.solve_steady_state`` hands the residual
 
 (one ``update()``, or ``iterate(dt)`` for a longer horizon) to SciPy's
 ``optimize.root(method="krylov")``: inexact Newton with an LGMRES inner solver
-and finite-difference Jacobian-vector products.  Here the same residual runs
-through the fused step and the Newton-Krylov iteration is written for the GPU:
+and finite-difference Jacobian-vector products.  Every evaluation also advances
+the solver's pressure ``NS.pres``, so F depends on the evaluation history.
+
+``solve_steady_state(method="reference")`` (the default) is exactly that: the
+same SciPy call on the same residual, each evaluation one step of the GPU path
+(the fused passes) with the pressure carried from evaluation to evaluation; it
+returns SciPy's result, as the reference does.
+
+``method="augmented"`` is this project's variant, written for the GPU:
 
 - the two evaluations of a central-difference Jacobian-vector product,
   F(X + eps v) and F(X - eps v), are two instances of one fused batch, so each
@@ -17,8 +24,9 @@ through the fused step and the Newton-Krylov iteration is written for the GPU:
 - Armijo backtracking on |F|.
 
 The reference carries the pressure through its residual (every evaluation
-advances ``NS.pres``), which makes F depend on the evaluation history.  Here
-the pressure is an unknown of the Newton iteration next to (T, U, V), with the
+advances ``NS.pres``), which makes F depend on the evaluation history (and
+keeps SciPy's iteration from converging on the cases tried).  In the augmented
+variant the pressure is an unknown of the Newton iteration next to (T, U, V), with the
 residual (pres' - pres) / dt of the step's pressure update, so F is one
 deterministic map and its zero is a fixed point of the complete step; the
 returned ``x`` keeps the reference's (T, U, V) layout and the solver's
@@ -55,17 +63,34 @@ class NavierStokesSteadyState:
         return torch.cat(self.flatten())
 
     def steady_fun(self, X, NS=None, dt=None):
-        """(Phi(X) - X) / dt on the plain path; advances NS's pressure, as the reference does."""
+        """(Phi(X) - X) / dt (rbc2d_base.py:321-341): one step, or the time loop over ``dt`` with the
+        clock reset around it; advances NS's pressure, as the reference does."""
         NS = self if NS is None else NS
         NS.T.vhat, NS.U.vhat, NS.V.vhat = NS.reshape(X)
         if dt is None:
             dt = NS.dt
             NS.update()
         else:
-            nsteps = int(round(dt / NS.dt))
-            for _ in range(nsteps):
-                NS.update()
+            NS.reset_time()
+            NS.iterate(dt, callback=False)
+            NS.reset_time()
         return (NS.vectorify() - X) / dt
+
+    def _solve_reference(self, X0, dt, maxiter, disp, tol, jac_options):
+        """SciPy's Newton-Krylov on steady_fun with the reference's options (rbc2d_base.py:266-294);
+        x travels between the host iteration and the device step once per evaluation."""
+        from scipy import optimize
+        options = {"maxiter": maxiter, "disp": disp, "fatol": tol, "jac_options": jac_options}
+        x0 = self.vectorify() if X0 is None else X0
+        x0 = x0.detach().cpu().numpy() if torch.is_tensor(x0) else np.asarray(x0, dtype=np.float64)
+        dev = self.T.vhat.device
+
+        def fun(x, NS, dt):
+            return NS.steady_fun(torch.as_tensor(x, dtype=torch.float64, device=dev), NS, dt).cpu().numpy()
+
+        if disp:
+            print("\nSolve steady state ...\n")
+        return optimize.root(fun, x0, args=(self, dt), method="krylov", options=options)
 
     # -- Newton-Krylov on the fused step
     def _pair(self):
@@ -94,8 +119,17 @@ class NavierStokesSteadyState:
         return outs
 
     def solve_steady_state(self, X0=None, dt=None, maxiter=300, disp=True, tol=1e-8,
-                           jac_options={"inner_maxiter": 30}):  # noqa: B006 (the reference's signature)
-        """Newton-Krylov for F = 0 (rbc2d_base.py:266-294); ``tol`` bounds max|F| like scipy's fatol."""
+                           jac_options={"inner_maxiter": 30}, method="reference"):  # noqa: B006
+        """Newton-Krylov for F = 0 (rbc2d_base.py:266-294); ``tol`` bounds max|F| like scipy's fatol.
+
+        ``method="reference"``: SciPy's iteration on the reference's residual (the pressure carried
+        through the evaluations); returns SciPy's OptimizeResult.  ``method="augmented"``: the GPU
+        Newton-Krylov with the pressure as an unknown (module docstring); returns a
+        SteadyStateResult with x on the device."""
+        if method == "reference":
+            return self._solve_reference(X0, dt, maxiter, disp, tol, jac_options)
+        if method != "augmented":
+            raise ValueError("method must be 'reference' or 'augmented'")
         if self.nstage != 1:
             raise NotImplementedError("the fused residual covers IMEX Euler")
         nsteps = 1 if dt is None else int(round(dt / self.dt))
