@@ -7,6 +7,7 @@ to the device.  ``write`` / ``read`` keep the reference's snapshot layout
 import numpy as np
 import torch
 
+from . import _lib
 from ._dev import to_dev, DTYPE, device
 from .bases import MetaBase
 from .spectralspace import SpectralSpace, SpectralSpaceBC
@@ -28,34 +29,67 @@ def zero_unpad(array, target_length, axis=0):
     return array.narrow(axis, 0, target_length)
 
 
-class FieldBase:
-    """Transforms shared by Field and FieldBC (field.py:9-56)."""
+def _on_axis(t, axis, fn):
+    """``fn`` (a 1-D operator along axis 0) applied along ``axis`` of ``t`` through a transposed
+    view: the C ABI takes strides, so nothing is copied."""
+    return fn(t) if axis == 0 else fn(t.transpose(axis, 0)).transpose(axis, 0)
 
-    def forward(self, v=None, undealias_after=None):
-        vhat = self.v if v is None else to_dev(v)
-        if undealias_after is None:
-            undealias_after = self.dealiased_space
-        for axis in range(self.ndim):
-            vhat = self.forward_fft(vhat, axis=axis)
-            if undealias_after:
-                vhat = zero_unpad(vhat, self.size_undealiased[axis], axis=axis)
-        if v is None:
-            self.vhat = vhat
-        else:
-            return vhat
+
+def _values(coef_base, grid_base, c):
+    """Coefficient lines of ``coef_base`` -> values on ``grid_base``'s points (axis 0).  A shorter
+    coefficient base (the undealiased one) is not padded by a copy: the stencil maps its own
+    coefficients to Chebyshev ones, and the backward DCT of the grid's length reads those and
+    zero-fills the rest of the line (the kernel's input length, like the fused passes' SETLEN).
+    Zero-padding commutes with the Shen stencils, whose entries depend on the row index only."""
+    u = coef_base.to_chebyshev(c) if hasattr(coef_base, "to_chebyshev") else _as_lines(c)
+    fam = getattr(grid_base, "family", grid_base)
+    return fam._dct(u, _lib.DCT_BWD)
+
+
+def _as_lines(t):
+    if t.dim() not in (1, 2):
+        raise NotImplementedError("ndim must be less than 3")
+    return t
+
+
+class FieldBase:
+    """Transforms shared by Field and FieldBC (field.py:9-56).
+
+    Axis 0 then axis 1, each one strided C-ABI pass over a view.  A 3/2-dealiased field keeps
+    its undealiased twin's bases (``_coef_bases``): a backward transform reads coefficients of
+    either length (the short ones are zero-filled inside the DCT, no padded copy), a forward one
+    returns the leading coefficients of the long transform as a view (the truncation)."""
+
+    def _coef_base(self, axis, n):
+        grid = self.xs[axis]
+        if n == grid.M:
+            return grid
+        short = getattr(self, "_coef_bases", None)
+        if short is not None and n == short[axis].M:
+            return short[axis]
+        raise ValueError("axis %d: %d coefficients, the field has %d%s" % (
+            axis, n, grid.M, "" if short is None else " or %d" % short[axis].M))
 
     def backward(self, vhat=None, dealias_before=None):
-        v = self.vhat if vhat is None else to_dev(vhat)
-        if dealias_before is None:
-            dealias_before = self.dealiased_space
+        data = self.vhat if vhat is None else to_dev(vhat)
+        pad = self.dealiased_space if dealias_before is None else dealias_before
+        for axis, grid in enumerate(self.xs):
+            n = data.shape[axis]
+            coef = self._coef_base(axis, n) if (pad or n != grid.M) else grid
+            data = _on_axis(data, axis, lambda t, c=coef, g=grid: _values(c, g, t))
+        if vhat is not None:
+            return data
+        self.v = data
+
+    def forward(self, v=None, undealias_after=None):
+        data = self.v if v is None else to_dev(v)
+        cut = self.dealiased_space if undealias_after is None else undealias_after
+        keep = self.size_undealiased if cut else [b.M for b in self.xs]
         for axis in range(self.ndim):
-            if dealias_before:
-                v = zero_pad(v, self.xs[axis].M, axis=axis)
-            v = self.backward_fft(v, axis=axis)
-        if vhat is None:
-            self.v = v
-        else:
-            return v
+            data = self.forward_fft(data, axis=axis).narrow(axis, 0, keep[axis])
+        if v is not None:
+            return data
+        self.vhat = data
 
     @property
     def v(self):
@@ -112,46 +146,64 @@ class Field(SpectralSpace, FieldBase):
         self.vhat = np.zeros(self.shape_spectral)
         self.field_bc = None
         self.t = 0
-        self.V = []
-        self.T = []
+        self._history = []
         self.dealiased_space = False
         self.create_dealiased_field(bases)
 
     def create_dealiased_field(self, bases):
-        if all(hasattr(i, "dealias") for i in bases):
-            self.dealias = Field([i.dealias for i in bases])
-            self.dealias.size_undealiased = [self.xs[i].M for i in range(self.ndim)]
-            self.dealias.dealiased_space = True
+        """The 3/2-grid twin (field.py:271-276): its own bases are the dealiased ones; it reads and
+        returns coefficients of this field's size."""
+        if not all(hasattr(b, "dealias") for b in bases):
+            return
+        twin = Field([b.dealias for b in bases])
+        twin._coef_bases = list(self.xs)
+        twin.size_undealiased = list(self.shape_spectral)
+        twin.dealiased_space = True
+        self.dealias = twin
 
     def add_field_bc(self, field_bc):
-        assert isinstance(field_bc, FieldBC)
+        if not isinstance(field_bc, FieldBC):
+            raise AssertionError("add_field_bc expects a FieldBC")
         self.field_bc = field_bc
 
-    def make_homogeneous(self):
-        if self.field_bc is None:
-            import warnings
-            warnings.warn("No inhomogeneous field found. Call add_bc(bchat,axis) first!")
-        return self.v - self.inhomogeneous
-
+    # the field splits into the part that meets homogeneous conditions (v) and the lift that
+    # carries the boundary values (the FieldBC's v); without a lift the latter is zero
     @property
-    def total(self):
-        return self.homogeneous + self.inhomogeneous
+    def inhomogeneous(self):
+        return 0 if self.field_bc is None else self.field_bc.v
 
     @property
     def homogeneous(self):
         return self.v
 
     @property
-    def inhomogeneous(self):
-        if self.field_bc is not None:
-            return self.field_bc.v
-        return 0
+    def total(self):
+        lift = self.inhomogeneous
+        return self.v if isinstance(lift, int) else torch.add(self.v, lift)
+
+    def make_homogeneous(self):
+        """v minus the lift (field.py:286-291); warns when no FieldBC was added."""
+        if self.field_bc is None:
+            import warnings
+            warnings.warn("No inhomogeneous field found. Call add_bc(bchat,axis) first!")
+            return self.v
+        return torch.sub(self.v, self.field_bc.v)
+
+    # time history kept by save(): (time, device copy of v) pairs; V and T are their columns
+    @property
+    def V(self):
+        return [v for _, v in self._history]
+
+    @property
+    def T(self):
+        return [t for t, _ in self._history]
 
     def save(self, transform=True):
+        """Append (t, v) to the history (field.py:323-330); v is brought up to date first unless
+        ``transform`` is False."""
         if transform:
             self.backward()
-        self.V.append(self.v.clone())
-        self.T.append(self.t)
+        self._history.append((self.t, self.v.clone()))
 
     def write(self, filename="file_0.h5", dict=None, leading_str="flow", add_time=True,  # noqa: A002
               grp_name=""):
@@ -187,18 +239,24 @@ class FieldBC(SpectralSpaceBC, FieldBase):
 
 
 class MultiField:
-    """Collection of fields updated together (field.py:417-465)."""
+    """Fields stepped and saved together under group names (field.py:417-465)."""
 
     def __init__(self, fields, names):
-        self.fields, self.names = [], []
-        for f, n in zip(fields, names):
-            if not isinstance(f, Field):
-                raise ValueError("Must be of type Field.")
-            self.fields.append(f)
-            self.names.append(n)
+        bad = [type(f).__name__ for f in fields if not isinstance(f, Field)]
+        if bad:
+            raise ValueError("Must be of type Field.")
+        self._by_name = dict(zip(names, fields))
+
+    @property
+    def fields(self):
+        return list(self._by_name.values())
+
+    @property
+    def names(self):
+        return list(self._by_name)
 
     def save(self):
-        for f in self.fields:
+        for f in self._by_name.values():
             f.save()
 
     def write(self, filename=None, leading_str="", add_time=True, dict={}):  # noqa: A002, B006
@@ -219,5 +277,6 @@ class MultiField:
                 io.read_field(f, st, n, dict)
 
     def update_time(self, dt):
-        for f in self.fields:
+        """Advance every field's clock by dt (field.py:462-465)."""
+        for f in self._by_name.values():
             f.t += dt

@@ -1,10 +1,12 @@
 """Rayleigh-Benard IMEX time stepper on the GPU (navier/rbc2d.py, navier/rbc2d_base.py).
 
-``NavierStokes.update()`` follows the reference operation by operation: every
-pypde call (grad, convective_term, solver plans) becomes one or a few launches
-of the pgx kernels.  This is the *plain* path.  ``NavierStokes.fused()``
-returns the same step as ~10 fused line-program passes that can be replayed
-from a CUDA graph (``pypde_gb300.navier.fused``).
+``NavierStokes.update()`` takes one time step.  Unless autograd records
+through the state it runs the fused form (``NavierStokes.fused()``): the same
+step as about a dozen fused line-program passes that can be replayed from a
+CUDA graph (``pypde_gb300.navier.fused``).  ``update(fused=False)`` follows the
+reference operation by operation, every pypde call (grad, convective_term,
+solver plans) one or a few launches of the pgx kernels: the *plain* path, which
+``torch.autograd`` differentiates.
 """
 import numpy as np
 import torch
@@ -246,8 +248,24 @@ class NavierStokes(NavierStokesBase, NavierStokesSteadyState, Integrator):
         self.pres.vhat = self.pres.vhat - 1.0 * self.nu * div * self.beta
         self.pres.vhat = self.pres.vhat + 1.0 / (self.dt * self.a[stage]) * galerkin_to_cheby(self.P.vhat, self.P)
 
-    def update(self):
-        """One time step, plain path (rbc2d.py:396-434)."""
+    def _autograd_records(self):
+        return torch.is_grad_enabled() and any(getattr(self, k).vhat.requires_grad
+                                               for k in ("T", "U", "V", "P", "pres"))
+
+    def update(self, fused=None):
+        """One time step (rbc2d.py:396-434).  ``fused=None``: the fused step (``fused()``; the same
+        operators regrouped by axis, equal to the plain path to rounding) unless autograd records
+        through the state, then the plain path; ``fused=False``: the plain path, operation by
+        operation (``update_plain``)."""
+        if fused is None:
+            fused = not self._autograd_records()
+        if fused:
+            self.fused().step()
+        else:
+            self.update_plain()
+
+    def update_plain(self):
+        """One time step operation by operation, as the reference runs it (rbc2d.py:396-434)."""
         self.ux_old, self.uz_old = 0, 0
         for rk in range(self.nstage):
             That = galerkin_to_cheby(self.T.vhat, self.T) + self.Tbc_cheby
@@ -288,12 +306,12 @@ class NavierStokes(NavierStokesBase, NavierStokesSteadyState, Integrator):
     def iterate(self, maxtime, callback=True, fused=None):
         """The time loop of integrator.py:14-32 (steps, time, save / callback every ``tsave``).  The
         steps are replays of the fused step's CUDA graph (``fused=None``: whenever autograd is not
-        recording through the state), else ``update()``; both give the reference's step."""
+        recording through the state), else plain ``update(fused=False)`` steps; both give the
+        reference's step."""
         if fused is None:
-            fused = not (torch.is_grad_enabled() and any(getattr(self, k).vhat.requires_grad
-                                                         for k in ("T", "U", "V", "P", "pres")))
+            fused = not self._autograd_records()
         if not fused:
-            return Integrator.iterate(self, maxtime, callback)
+            return Integrator.iterate(self, maxtime, callback, fused=False)
         f = self.fused()
         if f.graph is None:
             f.capture(1)

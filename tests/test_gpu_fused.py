@@ -100,7 +100,7 @@ def test_fused_matches_plain(NS):
     a.set_temperature_noise(4, 1e-2)
     b.set_temperature_noise(4, 1e-2)
     for _ in range(5):
-        a.update()
+        a.update(fused=False)
     b.update_fused(5)
     sa, sb = a.state(), b.state()
     for k in sa:

@@ -197,19 +197,22 @@ RBC = [
 ]
 
 
+@pytest.mark.parametrize("fused", [False, None], ids=["plain", "default"])
 @pytest.mark.parametrize("case", RBC, ids=[c[0] for c in RBC])
-def test_rbc2d_plain_golden(pg, golden, case):
+def test_rbc2d_plain_golden(pg, golden, case, fused):
+    """update(fused=False): the operation-by-operation path; update(): the default (fused) step."""
     from pypde_gb300.navier.rbc2d import NavierStokes
     tag, kind, shape, cfg, nsteps, seed, amp = case
     ns = NavierStokes(case=kind, shape=shape, pr=1.0, tsave=None, **cfg)
     ns.set_temperature_noise(seed, amp)
     assert rel_err(host(ns.T.vhat), golden[tag + "_T0"]) < TOL
-    ns.update()
+    ns.update(fused=fused)
+    assert (ns._fused is None) == (fused is False)
     st = ns.state()
     for name in ("T", "U", "V", "P", "pres"):
         assert rel_err(st[name], golden[f"{tag}_s1_{name}"]) < 1e-9, name
     for _ in range(nsteps - 1):
-        ns.update()
+        ns.update(fused=fused)
     st = ns.state()
     for name in ("T", "U", "V", "P", "pres"):
         assert rel_err(st[name], golden[f"{tag}_s{nsteps}_{name}"]) < 1e-8, name
