@@ -86,7 +86,7 @@ extern "C" int pgx_cheb_transform_2d_noalloc(const double* in, int64_t in_s0, in
                                              int32_t n1_in, double* out, int64_t out_s0, int64_t out_s1,
                                              int32_t n0_out, int32_t n1_out, int32_t N0, int32_t N1, int32_t mode,
                                              void* stream) {
-  if (!in || !out || mode < 0 || mode > 2 || N0 < 3 || N1 < 3 || N0 > PGX_LMAX - 8 || N1 > PGX_LMAX - 8 ||
+  if (!in || !out || mode < 0 || mode > 2 || N0 < 2 || N1 < 2 || N0 > PGX_LMAX - 8 || N1 > PGX_LMAX - 8 ||
       n0_in < 0 || n0_in > N0 || n1_in < 0 || n1_in > N1 || n0_out < 0 || n0_out > N0 || n1_out < 0 ||
       n1_out > N1)
     return PGX_E_ARG;
