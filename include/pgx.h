@@ -96,6 +96,11 @@ enum pgx_opcode {
 
 /* DCT modes; FWD_T and BWD_T are the exact transposes (adjoints) of FWD and BWD. */
 enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_FWD_T = 3, PGX_DCT_BWD_T = 4 };
+/* op.k of DCT: the mode in the low bits; PGX_DCT_CTA runs an even-length transform with its
+ * phases spread over the whole CTA (block barriers between FFT stages) instead of one warp per
+ * line pair. */
+#define PGX_DCT_MODE_MASK 7
+#define PGX_DCT_CTA 8
 
 /* Chain ops (DIFF, TDMA2, FDMA) act on the b consecutive slots a..a+b-1 at
  * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset.
@@ -149,6 +154,50 @@ int pgx_check_instance(const pgx_program* prog, const pgx_instance* inst);
 int pgx_run_batched(const pgx_program* prog, const pgx_instance* d_insts,
                     const int32_t* d_work, int32_t nwork, void* stream);
 
+/* ------------------------------------------------------- persistent steps
+ * No counterpart in the reference (its time loop is integrator.py:14-32, one
+ * instance, one operation at a time).  Many passes of many instances -- whole
+ * time steps of a batch -- in ONE launch: every CTA takes the next work item
+ * from a queue (an atomic counter over `items`, which are in an order where
+ * every item comes after the items it depends on), waits until the counter it
+ * depends on has reached its target, runs the item's program on one tile of
+ * one instance descriptor, and adds one to the counter it completes.  An
+ * instance starts its next pass (or its next step) as soon as its own previous
+ * pass is complete, not when every instance's is.
+ *
+ * Item fields: prog (index into the programs), desc (index into the
+ * descriptors), tile, wait (counter index, or -1: no dependency), need (the
+ * count `wait` must reach), done (counter index completed by this item).
+ * A wait that has not been satisfied after `spin_limit` SM clock cycles ends
+ * the launch with PGX_PERSIST_TIMEOUT in state[1] and the item index in
+ * state[2]; an item with an out-of-range index ends it with
+ * PGX_PERSIST_BAD_ITEM.  The call resets the `ncounters` counters and the
+ * three state words (next item, error, where) on `stream` before the launch,
+ * so it can be recorded in a CUDA graph and replayed; pgx_persist_error reads
+ * the error word (synchronising the stream).
+ *
+ * h_progs (HOST) are checked like pgx_run's programs; d_progs must hold the
+ * same nprogs programs in DEVICE memory.  d_descs (ndescs), d_items, d_counters
+ * and d_state (3 int32) are DEVICE memory; every descriptor must pass
+ * pgx_check_instance with the programs its items name.  ctas = 0: as many CTAs
+ * as fit on the device at once; threads = 0: the largest nthreads of the
+ * programs (every program runs with the launch's CTA size). */
+typedef struct pgx_persist_item {
+  int32_t prog, desc, tile, wait, need, done;
+} pgx_persist_item;
+#define PGX_PERSIST_TIMEOUT 1
+#define PGX_PERSIST_BAD_ITEM 2
+int pgx_run_persistent(const pgx_program* h_progs, const pgx_program* d_progs, int32_t nprogs,
+                       const pgx_instance* d_descs, int32_t ndescs, const pgx_persist_item* d_items,
+                       int32_t nitems, int32_t* d_counters, int32_t ncounters, int32_t* d_state,
+                       int32_t ctas, int32_t threads, int64_t spin_limit, void* stream);
+/* The launch shape pgx_run_persistent uses for these programs: CTA size, CTAs
+ * resident per SM and dynamic shared memory per CTA (bytes). */
+int pgx_persistent_shape(const pgx_program* h_progs, int32_t nprogs, int32_t threads, int32_t* out_threads,
+                         int32_t* out_ctas_per_sm, int64_t* out_smem);
+/* state[1] (0 = the last launch completed every item), synchronising `stream`. */
+int pgx_persist_error(const int32_t* d_state, int32_t* error, int32_t* where, void* stream);
+
 /* ------------------------------------------------ reference-facing kernels */
 
 /* DCT-I along `axis` of an n0 x n1 array, in -> out (may alias).
@@ -181,7 +230,8 @@ int pgx_cheb_transform_2d(const double* in, int64_t in_s0, int64_t in_s1, int32_
  * the scratch between the two axis passes (at most PGX_NOALLOC_SCRATCH_DOUBLES =
  * n0_out * n1_in doubles, 16 MiB) and the twiddle tables live in static device
  * arrays that every GPU loading the library holds until exit.  Lengths N0, N1
- * must have n-1 = 2^a 3^b (FFT plans only).  Larger or other sizes return
+ * (2 <= N <= PGX_LMAX - 8, as for pgx_cheb_transform_2d) must have n-1 = 2^a 3^b
+ * (FFT plans only).  Larger or other sizes return
  * PGX_E_ARG before any launch.  It calls no cudaMalloc, cudaFree or other
  * allocating routine.  The first call on a device looks up the arrays' device
  * addresses (cudaGetSymbolAddress); make that first call before any stream
@@ -296,6 +346,15 @@ int pgx_matrix_plan_is_banded(const pgx_matrix_plan* plan);
  * DCT-I of n points, and the stencil sub-diagonal table.  The returned device
  * pointer is owned by the library and valid until process exit. */
 int pgx_dct_table(int32_t n, const double** table);
+
+/* ------------------------------------------------------------ measurement
+ * No counterpart in the reference: the FP64 roofline denominator.  Launches
+ * `ctas` x `threads` threads that each run 8 independent FMA chains of `iters`
+ * steps and store one double (out: ctas * threads doubles of device memory);
+ * the caller times it with events on `stream`.  pgx_fp64_fma_probe_flops gives
+ * the flops of one launch (an FMA counts two). */
+int pgx_fp64_fma_probe(double* out, int32_t ctas, int32_t threads, int32_t iters, void* stream);
+int64_t pgx_fp64_fma_probe_flops(int32_t ctas, int32_t threads, int32_t iters);
 
 #ifdef __cplusplus
 }

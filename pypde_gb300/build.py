@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpypde_gb300.so")
-SOURCES = ["pgx_kernels.cu", "pgx_api.cu", "pgx_noalloc.cu"]
+SOURCES = ["pgx_kernels.cu", "pgx_api.cu", "pgx_noalloc.cu", "pgx_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -20,6 +20,11 @@ namespace pgx {
 int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles);
 int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
                    cudaStream_t s);
+int persistent_shape(const pgx_program* progs, int nprogs, int threads, int* out_threads, int* ctas_per_sm,
+                     int64_t* smem);
+int launch_persistent(const pgx_program* d_progs, int nprogs, const pgx_instance* d_descs, int ndescs,
+                      const pgx_persist_item* d_items, int nitems, int32_t* d_counters, int ncounters,
+                      int32_t* d_state, int ctas, int threads, int64_t smem, long long spin_limit, cudaStream_t s);
 }
 
 static thread_local int g_last_cuda = 0;
@@ -173,6 +178,61 @@ extern "C" int pgx_run_batched(const pgx_program* P, const pgx_instance* d_insts
   if (nwork == 0) return PGX_OK;
   int e = pgx::launch_batched(P, d_insts, d_work, nwork, (cudaStream_t)stream);
   if (e) return cuda_fail((cudaError_t)e);
+  return PGX_OK;
+}
+
+// --------------------------------------------------------- persistent steps
+extern "C" int pgx_persistent_shape(const pgx_program* h_progs, int32_t nprogs, int32_t threads, int32_t* out_threads,
+                                    int32_t* out_ctas_per_sm, int64_t* out_smem) {
+  if (!h_progs || nprogs < 1 || threads < 0 || threads > PGX_MAX_THREADS_FFT || (threads & 31) || !out_threads ||
+      !out_ctas_per_sm || !out_smem)
+    return PGX_E_ARG;
+  for (int i = 0; i < nprogs; ++i) {
+    int rc = check_program_shape(h_progs + i);
+    if (rc) return rc;
+  }
+  int nt = 0, per = 0;
+  int64_t smem = 0;
+  int e = pgx::persistent_shape(h_progs, nprogs, threads, &nt, &per, &smem);
+  if (e) return cuda_fail((cudaError_t)e);
+  if (nt > PGX_MAX_THREADS_FFT || smem > smem_optin_max()) return PGX_E_SMEM;
+  *out_threads = nt;
+  *out_ctas_per_sm = per;
+  *out_smem = smem;
+  return PGX_OK;
+}
+
+extern "C" int pgx_run_persistent(const pgx_program* h_progs, const pgx_program* d_progs, int32_t nprogs,
+                                  const pgx_instance* d_descs, int32_t ndescs, const pgx_persist_item* d_items,
+                                  int32_t nitems, int32_t* d_counters, int32_t ncounters, int32_t* d_state,
+                                  int32_t ctas, int32_t threads, int64_t spin_limit, void* stream) {
+  if (!d_progs || !d_descs || ndescs < 1 || nitems < 0 || (nitems > 0 && !d_items) || !d_counters || ncounters < 1 ||
+      !d_state || ctas < 0 || spin_limit < 1)
+    return PGX_E_ARG;
+  int nt = 0, per = 0;
+  int64_t smem = 0;
+  int rc = pgx_persistent_shape(h_progs, nprogs, threads, &nt, &per, &smem);
+  if (rc) return rc;
+  if (per < 1) return PGX_E_SMEM;
+  int dev = 0, sms = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ce != cudaSuccess) return cuda_fail(ce);
+  const int grid = ctas > 0 ? ctas : per * sms;
+  int e = pgx::launch_persistent(d_progs, nprogs, d_descs, ndescs, d_items, nitems, d_counters, ncounters, d_state,
+                                 grid, nt, smem, (long long)spin_limit, (cudaStream_t)stream);
+  if (e) return cuda_fail((cudaError_t)e);
+  return PGX_OK;
+}
+
+extern "C" int pgx_persist_error(const int32_t* d_state, int32_t* error, int32_t* where, void* stream) {
+  if (!d_state || !error) return PGX_E_ARG;
+  int32_t h[3] = {0, 0, 0};
+  cudaError_t e = cudaMemcpyAsync(h, d_state, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e);
+  *error = h[1];
+  if (where) *where = h[2];
   return PGX_OK;
 }
 

@@ -17,6 +17,7 @@
 // (banded sweeps read x[i+2], x[i+4]) without branches.
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include <mutex>
@@ -433,26 +434,53 @@ __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 // One warp per (slot, line): each lane owns a contiguous chunk, the chunk totals of
 // both parity classes are suffix-scanned across the warp, then every lane walks its
 // chunk backwards.  Depth ~ n/32 + 5 dependent adds instead of n.
+// lanes per line for per-line phases of a warp that owns nl lines (2 <= L <= 32): the warp's
+// 32 lanes cover all its lines at once
+__device__ __forceinline__ int lanes_per_line(int nl) {
+  int L = 32;
+  while (L > 2 && L * nl > 32) L >>= 1;
+  return L;
+}
+
+// Lines of a per-line op over ns slots: warp w takes lines [w per, (w + 1) per), then every
+// nw * per further; L lanes a line (the lanes of one line form an aligned group of L).
+struct LineLanes {
+  int L, per, grp, sub, first, stride, nl;
+};
+__device__ __forceinline__ LineLanes line_lanes(const Ctx& c, int nl) {
+  LineLanes g;
+  const int nw = c.nthreads >> 5, lane = c.tid & 31;
+  g.L = lanes_per_line((nl + nw - 1) / nw);
+  g.per = 32 / g.L;
+  g.grp = lane / g.L;
+  g.sub = lane & (g.L - 1);
+  g.first = (c.tid >> 5) * g.per;
+  g.stride = nw * g.per;
+  g.nl = nl;
+  return g;
+}
+
 __device__ void op_diff(Ctx& c, const pgx_op& op) {
   const int ns = nslot_of(op);
-  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
-  for (int w = warp; w < ns * c.tb; w += nw) {
-    const int s = w / c.tb, t = w - s * c.tb;
-    const int n = c.slen[op.a + s];
+  const LineLanes g = line_lanes(c, ns * c.tb);
+  for (int base = g.first; base < g.nl; base += g.stride) {  // the same trip count for the whole warp
+    const int w = base + g.grp;
+    const bool valid = w < g.nl;
+    const int s = valid ? w / c.tb : 0, t = valid ? w - s * c.tb : 0;
+    const int n = valid ? c.slen[op.a + s] : 0;
     double* x = slot_ptr(c, op.a + s) + t * c.lcap;
-    const int chunk = (n + 31) >> 5;
-    const int a = lane * chunk, b = min(a + chunk, n);
+    const int chunk = (n + g.L - 1) / g.L;
+    const int a = min(g.sub * chunk, n), b = min(a + chunk, n);
     for (int rep = 0; rep < op.k; ++rep) {
       double tot[2] = {0.0, 0.0};
       for (int i = a; i < b; ++i) tot[i & 1] = fma(c_twok.v[i], x[i], tot[i & 1]);
-      const double c1 = x[1];
-      // exclusive suffix sums of the chunk totals over the lanes above this one
+      const double c1 = valid ? x[1] : 0.0;
+      // exclusive suffix sums of the chunk totals over the lanes above this one (of this line)
       double in0 = tot[0], in1 = tot[1];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const double v0 = __shfl_down_sync(0xffffffffu, in0, o);
-        const double v1 = __shfl_down_sync(0xffffffffu, in1, o);
-        if (lane + o < 32) {
+      for (int o = 1; o < g.L; o <<= 1) {
+        const double v0 = __shfl_down_sync(0xffffffffu, in0, o, g.L);
+        const double v1 = __shfl_down_sync(0xffffffffu, in1, o, g.L);
+        if (g.sub + o < g.L) {
           in0 += v0;
           in1 += v1;
         }
@@ -465,7 +493,7 @@ __device__ void op_diff(Ctx& c, const pgx_op& op) {
         acc[i & 1] += wi;
       }
       __syncwarp();
-      if (lane == 0) x[0] = fma(0.5, n > 2 ? x[2] : 0.0, c1);
+      if (valid && g.sub == 0) x[0] = fma(0.5, n > 2 ? x[2] : 0.0, c1);
       __syncwarp();
     }
   }
@@ -473,26 +501,27 @@ __device__ void op_diff(Ctx& c, const pgx_op& op) {
 
 // Transpose of the derivative recurrence (adjoint of op_diff), in place:
 //   (D^T y)_i = 2i sum_{1 <= j < i, j = i+1 mod 2} y_j + y_0 [i odd] (1 if i = 1 else i).
-// Warp-parallel forward prefix sums per parity class.
+// Forward prefix sums per parity class, L lanes a line.
 __device__ void op_diff_t(Ctx& c, const pgx_op& op) {
   const int ns = nslot_of(op);
-  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
-  for (int w = warp; w < ns * c.tb; w += nw) {
-    const int s = w / c.tb, t = w - s * c.tb;
-    const int n = c.slen[op.a + s];
+  const LineLanes g = line_lanes(c, ns * c.tb);
+  for (int base = g.first; base < g.nl; base += g.stride) {
+    const int w = base + g.grp;
+    const bool valid = w < g.nl;
+    const int s = valid ? w / c.tb : 0, t = valid ? w - s * c.tb : 0;
+    const int n = valid ? c.slen[op.a + s] : 0;
     double* x = slot_ptr(c, op.a + s) + t * c.lcap;
-    const int chunk = (n + 31) >> 5;
-    const int a = lane * chunk, b = min(a + chunk, n);
+    const int chunk = (n + g.L - 1) / g.L;
+    const int a = min(g.sub * chunk, n), b = min(a + chunk, n);
     for (int rep = 0; rep < op.k; ++rep) {
       double tot[2] = {0.0, 0.0};
       for (int i = max(a, 1); i < b; ++i) tot[i & 1] += x[i];
-      const double y0 = x[0];
+      const double y0 = valid ? x[0] : 0.0;
       double in0 = tot[0], in1 = tot[1];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const double v0 = __shfl_up_sync(0xffffffffu, in0, o);
-        const double v1 = __shfl_up_sync(0xffffffffu, in1, o);
-        if (lane >= o) {
+      for (int o = 1; o < g.L; o <<= 1) {
+        const double v0 = __shfl_up_sync(0xffffffffu, in0, o, g.L);
+        const double v1 = __shfl_up_sync(0xffffffffu, in1, o, g.L);
+        if (g.sub >= o) {
           in0 += v0;
           in1 += v1;
         }
@@ -965,13 +994,14 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
 // tw is the table exp(-2 pi i k / (2N)): W_N^k = tw[2k], (cos, -sin)(pi j / N) = tw[j].
 // The backward pre-scale (-1)^j w_j is common to x_j and x_{N-j} (N even) and
 // applied to u_j, d_j; the forward post-scale to the outputs.
-__device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+__device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   // op.b > 1: the transforms of slots a .. a+b-1 (same length and mode) go through every
   // phase together: one barrier per phase for all of them, b times the parallel work.
   const int ns = nslot_of(op);
   const int n = c.slen[op.a];
   const int N = n - 1, H = N / 2;
-  const DctScale ds = dct_scale(op.k, N);
+  const int mode = op.k & PGX_DCT_MODE_MASK;
+  const DctScale ds = dct_scale(mode, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   const int npairs = (c.tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
@@ -983,7 +1013,7 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   // y_1: one warp per line (line lt = sl * tb + t)
   {
     const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
-    const bool alt = op.k == PGX_DCT_BWD || op.k == PGX_DCT_FWD_T;
+    const bool alt = mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T;
     const double ps = ds.has_pre ? (alt ? -ds.pre(1, N) : ds.pre(1, N)) : 1.0;
     for (int lt = warp; lt < ns * c.tb; lt += nw) {
       const int sl = lt / c.tb, t = lt - sl * c.tb;
@@ -1076,6 +1106,265 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
 }
 
+// ---------------------------------------------------------- warp-local even DCT
+// The same folded half-length algorithm as op_dct_even_cta, with every phase of a line pair
+// inside one warp: warp w owns the pairs P = w, w + nw, w + 2 nw, ... of all the op's slots and
+// runs their fold, FFT stages, untangle and scan separated by __syncwarp only, so the warps of a
+// CTA (and of the other CTAs on the SM) never wait for each other inside a transform.  Per line,
+// y_1 and the odd-coefficient scan use just enough lanes to cover the warp's lines (L lanes a
+// line, log2 L shuffle steps instead of 32 lanes and 5), and the fold is one FMA per point:
+// u_m = (x_m + x_{N-m})/2 - sin(pi m/N) (x_m - x_{N-m}) = x_{N-m} + (1/2 - sin(pi m/N)) (x_m - x_{N-m}).
+
+// Radix plan of the length-N FFT: every factor 3 first (the first stage has no twiddles, and a
+// twiddled radix-3 stage costs the most FP64 instructions per point), then 4s, then one 2.
+struct RadixPlan {
+  int n3, n4, n2;  // stages of radix 3, then 4, then 2
+  __device__ __forceinline__ int stages() const { return n3 + n4 + n2; }
+  __device__ __forceinline__ int at(int s) const { return s < n3 ? 3 : (s < n3 + n4 ? 4 : 2); }
+};
+__device__ __forceinline__ RadixPlan radix_plan(int N, int& rest) {
+  RadixPlan p{0, 0, 0};
+  int m = N;
+  while (m % 3 == 0) { ++p.n3; m /= 3; }
+  while (m % 4 == 0) { ++p.n4; m /= 4; }
+  if (m % 2 == 0) { ++p.n2; m /= 2; }
+  rest = m;  // 1 for every length with a twiddle table (n - 1 = 2^a 3^b)
+  return p;
+}
+
+struct WarpPairs {
+  int lane, w, nw, npw;  // lane, warp, warps of the CTA, pairs this warp owns
+};
+__device__ __forceinline__ WarpPairs warp_pairs(const Ctx& c, int nall) {
+  WarpPairs g;
+  g.lane = c.tid & 31;
+  g.w = c.tid >> 5;
+  g.nw = c.nthreads >> 5;
+  g.npw = g.w < nall ? (nall - g.w + g.nw - 1) / g.nw : 0;
+  return g;
+}
+
+template <int R>
+__device__ __forceinline__ void butterfly_plain(double2* v, double2* o) {
+  if (R == 2) {
+    o[0] = cadd(v[0], v[1]);
+    o[1] = csub(v[0], v[1]);
+  } else if (R == 4) {
+    double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
+    o[0] = cadd(a, e);
+    o[2] = csub(a, e);
+    o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
+    o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
+  } else {  // R == 3, W3 = -1/2 - i sqrt(3)/2
+    const double h = 0.86602540378443864676;
+    double2 t1 = cadd(v[1], v[2]);
+    double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
+    double2 t3 = csub(v[1], v[2]);
+    o[0] = cadd(v[0], t1);
+    o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));  // t2 - i h t3
+    o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));  // t2 + i h t3
+  }
+}
+
+// First stage (Ns = 1, no twiddles) with the fold on its way in, over the warp's pairs.
+template <int R>
+__device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2* dst, const double2* tw, int N,
+                                      int npairs, int slot0, const DctScale& ds) {
+  const int B = N / R;
+  for (int it = g.lane; it < g.npw * B; it += 32) {
+    const int q = it / B, j = it - q * B;
+    const int P = g.w + q * g.nw;
+    const int sl = P / npairs, pr = P - sl * npairs;
+    const double* x = slot_ptr(c, slot0 + sl);
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
+    double2 v[R], o[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int m = j + r * B;
+      const double cm = 0.5 + __ldg(&tw[m].y);  // 1/2 - sin(pi m / N)
+      const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
+      double ua = fma(cm, a0 - a1, a1);
+      double ub = 0.0;
+      if (two) {
+        const double b0 = x[(t0 + 1) * c.lcap + m], b1 = x[(t0 + 1) * c.lcap + N - m];
+        ub = fma(cm, b0 - b1, b1);
+      }
+      if (ds.has_pre) {
+        const double sg = ds.pre(m, N);
+        ua *= sg;
+        ub *= sg;
+      }
+      v[r] = make_double2(ua, ub);
+    }
+    butterfly_plain<R>(v, o);
+#pragma unroll
+    for (int q2 = 0; q2 < R; ++q2) dst[P * c.fft_stride + j * R + q2] = o[q2];
+  }
+}
+
+// One twiddled radix-R Stockham stage (Ns > 1) over the warp's pairs; tw holds exp(-2 pi i k / (tws L)).
+template <int R>
+__device__ __forceinline__ void wstage(const Ctx& c, const WarpPairs& g, const double2* src, double2* dst,
+                                       const double2* tw, int L, int Ns, int tws) {
+  const int B = L / R;
+  const int step = tws * (L / (Ns * R));
+  for (int it = g.lane; it < g.npw * B; it += 32) {
+    const int q = it / B, j = it - q * B;
+    const int P = g.w + q * g.nw;
+    const int k = j % Ns;
+    const double2* s = src + P * c.fft_stride;
+    double2 v[R], o[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = s[j + r * B];
+    if (R == 2) {
+      const double2 w1 = __ldg(tw + k * step);
+      o[0] = cmadd(v[0], w1, v[1]);
+      o[1] = ctwice_minus(v[0], o[0]);
+    } else if (R == 4) {
+      const double2 w1 = __ldg(tw + k * step), w2 = __ldg(tw + 2 * k * step);
+      const double2 a = cmadd(v[0], w2, v[2]), b = ctwice_minus(v[0], a);
+      const double2 cc = cmadd(v[1], w2, v[3]), d = ctwice_minus(v[1], cc);
+      o[0] = cmadd(a, w1, cc);
+      o[2] = ctwice_minus(a, o[0]);
+      o[1] = cmadd(b, make_double2(w1.y, -w1.x), d);
+      o[3] = ctwice_minus(b, o[1]);
+    } else {
+      if (k != 0) {
+        v[1] = cmul(v[1], __ldg(tw + k * step));
+        v[2] = cmul(v[2], __ldg(tw + 2 * k * step));
+      }
+      butterfly_plain<3>(v, o);
+    }
+    double2* d = dst + P * c.fft_stride + (j - k) * R + k;
+#pragma unroll
+    for (int q2 = 0; q2 < R; ++q2) d[q2 * Ns] = o[q2];
+  }
+}
+
+__device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int ns = nslot_of(op);
+  const int n = c.slen[op.a];
+  const int N = n - 1, H = N / 2;
+  const int mode = op.k & PGX_DCT_MODE_MASK;
+  const DctScale ds = dct_scale(mode, N);
+  const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
+  const int npairs = (c.tb + 1) >> 1;
+  const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
+  int rest = 1;
+  const RadixPlan plan = radix_plan(N, rest);
+  if (N > c.fft_stride || rest != 1 || plan.stages() < 1) {  // no buffer or plan for this length: refuse loudly
+    for (int sl = 0; sl < ns; ++sl)
+      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+    return;
+  }
+  const WarpPairs g = warp_pairs(c, nall);
+  if (g.npw == 0) return;
+  const int nl = 2 * g.npw;  // lines of the warp's pairs (the last one of an odd tile may not exist)
+  const int L = lanes_per_line(nl), per = 32 / L, grp = g.lane / L, sub = g.lane & (L - 1);
+
+  // y_1, L lanes a line: the j of a lane keep one parity (L even), so the alternating pre-scale
+  // of BWD / FWD_T is one sign per lane
+  {
+    const bool alt = mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T;
+    const double ps = ds.has_pre ? (alt ? -ds.pre(1, N) : ds.pre(1, N)) : 1.0;
+    const double p0 = ds.has_pre ? ds.pre(0, N) : 1.0;
+    for (int base = 0; base < nl; base += per) {
+      const int ll = base + grp, q = ll >> 1;
+      const int P = g.w + q * g.nw;
+      const int sl = P / npairs, t = 2 * (P - sl * npairs) + (ll & 1);
+      const bool valid = ll < nl && t < c.tb;
+      double acc = 0.0;
+      const double* xl = slot_ptr(c, op.a + (valid ? sl : 0)) + (valid ? t : 0) * c.lcap;
+      if (valid)
+        for (int j = 1 + sub; j < H; j += L) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
+      if (alt && ((1 + sub) & 1)) acc = -acc;
+      for (int o = L >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, L);
+      if (valid && sub == 0) c.ybuf[sl * c.tb + t] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
+    }
+  }
+  // FFT of length N over the warp's pairs, ping-pong between the two buffers
+  double2* bufs[2] = {c.f0, c.f1};
+  const int R0 = plan.at(0);
+  if (R0 == 3) wfold<3>(c, g, bufs[1], tw, N, npairs, op.a, ds);
+  else if (R0 == 4) wfold<4>(c, g, bufs[1], tw, N, npairs, op.a, ds);
+  else wfold<2>(c, g, bufs[1], tw, N, npairs, op.a, ds);
+  int cur = 1, Ns = R0;
+  for (int s = 1; s < plan.stages(); ++s) {
+    __syncwarp();
+    const int R = plan.at(s);
+    if (R == 4) wstage<4>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);
+    else if (R == 2) wstage<2>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);
+    else wstage<3>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);
+    cur ^= 1;
+    Ns *= R;
+  }
+  __syncwarp();
+  const double2* Z = bufs[cur];
+  // untangle: even outputs, odd increments (y_1 from the y_1 phase)
+  for (int it = g.lane; it < g.npw * (H + 1); it += 32) {
+    const int q = it / (H + 1), m = it - q * (H + 1);
+    const int P = g.w + q * g.nw;
+    const int sl = P / npairs, pr = P - sl * npairs;
+    double* x = slot_ptr(c, op.a + sl);
+    const int t0 = 2 * pr;
+    const bool two = t0 + 1 < c.tb;
+    const double2 zm = Z[P * c.fft_stride + m];
+    const double2 zn = Z[P * c.fft_stride + (m == 0 ? 0 : N - m)];
+    double ya = zm.x + zn.x, yb = zm.y + zn.y;
+    if (ds.has_post) {
+      const double sc = ds.post(2 * m, N);
+      ya *= sc;
+      yb *= sc;
+    }
+    x[t0 * c.lcap + 2 * m] = ya;
+    if (two) x[(t0 + 1) * c.lcap + 2 * m] = yb;
+    if (m >= 1 && m < H) {
+      x[t0 * c.lcap + 2 * m + 1] = zn.y - zm.y;
+      if (two) x[(t0 + 1) * c.lcap + 2 * m + 1] = zm.x - zn.x;
+    } else if (m == 0) {
+      x[t0 * c.lcap + 1] = c.ybuf[sl * c.tb + t0];
+      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
+    }
+  }
+  __syncwarp();
+  // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1, L lanes a line
+  {
+    const int chunk = (H + L - 1) / L;
+    const double osc = ds.has_post ? ds.post(1, N) : 1.0;  // the same for every odd k < N
+    for (int base = 0; base < nl; base += per) {
+      const int ll = base + grp, q = ll >> 1;
+      const int P = g.w + q * g.nw;
+      const int sl = P / npairs, t = 2 * (P - sl * npairs) + (ll & 1);
+      const bool valid = ll < nl && t < c.tb;
+      double* xl = slot_ptr(c, op.a + (valid ? sl : 0)) + (valid ? t : 0) * c.lcap;
+      const int m0 = min(sub * chunk, H), m1 = min(m0 + chunk, H);
+      double run = 0.0;
+      if (valid)
+        for (int m = m0; m < m1; ++m) run += xl[2 * m + 1];
+      double incl = run;
+      for (int o = 1; o < L; o <<= 1) {
+        const double v = __shfl_up_sync(0xffffffffu, incl, o, L);
+        if (sub >= o) incl += v;
+      }
+      if (!valid) continue;
+      double pre = incl - run;  // exclusive prefix of this lane's chunk
+      if (ds.has_post) {
+        for (int m = m0; m < m1; ++m) {
+          pre += xl[2 * m + 1];
+          xl[2 * m + 1] = pre * osc;
+        }
+      } else {
+        for (int m = m0; m < m1; ++m) {
+          pre += xl[2 * m + 1];
+          xl[2 * m + 1] = pre;
+        }
+      }
+    }
+  }
+}
+
 // DCT-I of the slot (length n) in place: the folded half-length algorithm for
 // even n - 1, otherwise paired lines through a length-2(n-1) FFT (stockham_stage).
 __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_instance& I);
@@ -1083,7 +1372,8 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
   if (((n - 1) & 1) == 0 && n >= 3) {
-    op_dct_even(c, op, I);
+    if (op.k & PGX_DCT_CTA) op_dct_even_cta(c, op, I);
+    else op_dct_even(c, op, I);
     return;
   }
   const int ns = nslot_of(op);  // paired-line path: one slot after the other
@@ -1100,7 +1390,7 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
     return;
   }
   const int N = n - 1, L = 2 * N;
-  const DctScale ds = dct_scale(op.k, N);
+  const DctScale ds = dct_scale(op.k & PGX_DCT_MODE_MASK, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, slot);
   const int npairs = (c.tb + 1) >> 1;
@@ -1145,9 +1435,9 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
 }
 
 // ------------------------------------------------------------------ driver
-template <bool BATCHED, bool FFT>
-__device__ void run_program(const pgx_program& P, const pgx_instance& I, int tile) {
-  extern __shared__ __align__(16) double smem_dyn[];
+// One tile of one instance: the program's ops on shared-memory slots that start at `sm`.
+template <bool FFT>
+__device__ void run_program(const pgx_program& P, const pgx_instance& I, int tile, double* sm) {
   Ctx c;
   c.tb = P.tb;
   c.lcap = P.lcap;
@@ -1156,7 +1446,7 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   c.l0 = tile * P.tb;
   c.nlines = I.len[P.lines_len];
   const int nbuf = P.nslots + 1;
-  c.sm = BATCHED ? smem_dyn + (sizeof(pgx_instance) + 7) / 8 : smem_dyn;
+  c.sm = sm;
   size_t off = (size_t)nbuf * c.tb * c.lcap;
   c.fft_stride = pgx_fft_stride(P.fft_n);
   const int fs = pgx_fft_slots(P);
@@ -1218,19 +1508,101 @@ __device__ __forceinline__ void run_batched(const pgx_program& P, const pgx_inst
   double* dst = reinterpret_cast<double*>(sI);
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
   __syncthreads();
-  run_program<true, FFT>(P, *sI, tile);
+  run_program<FFT>(P, *sI, tile, smem_dyn + (sizeof(pgx_instance) + 7) / 8);
+}
+
+// ------------------------------------------------------------- persistent steps
+// Shared memory of a persistent CTA: the current item's descriptor, its program, then the slots.
+constexpr int kPersistHead = (int)(((sizeof(pgx_instance) + 15) / 16 + (sizeof(pgx_program) + 15) / 16) * 16);
+
+__device__ __forceinline__ int ld_acquire_gpu(const int32_t* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_persistent(
+    const pgx_program* __restrict__ progs, int nprogs, const pgx_instance* __restrict__ descs, int ndescs,
+    const pgx_persist_item* __restrict__ items, int nitems, int32_t* __restrict__ counters, int ncounters,
+    int32_t* __restrict__ state, long long spin_limit) {
+  extern __shared__ __align__(16) double smem_dyn[];
+  pgx_instance* sI = reinterpret_cast<pgx_instance*>(smem_dyn);
+  pgx_program* sP = reinterpret_cast<pgx_program*>(reinterpret_cast<char*>(smem_dyn) +
+                                                   ((sizeof(pgx_instance) + 15) / 16) * 16);
+  double* slots = smem_dyn + kPersistHead / 8;
+  __shared__ int s_item, s_go;
+  volatile int32_t* err = state + 1;
+  // thread 0 holds the index of the CTA's next item: taken from the queue while the current item
+  // runs, so the atomic's latency hides behind the tile (items are still taken in list order, and a
+  // CTA holds its next item only while it runs one below it: the lowest unfinished item can always run)
+  int next = 0;
+  if (threadIdx.x == 0) next = atomicAdd(state, 1);
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int it = *err ? nitems : next;
+      int go = it < nitems;
+      if (go) {
+        const pgx_persist_item w = items[it];
+        if (w.prog < 0 || w.prog >= nprogs || w.desc < 0 || w.desc >= ndescs || w.done < 0 || w.done >= ncounters ||
+            w.wait >= ncounters || w.tile < 0) {
+          atomicCAS(state + 1, 0, PGX_PERSIST_BAD_ITEM);
+          state[2] = it;
+          go = 0;
+        } else if (w.wait >= 0) {
+          // bounded wait for the items this one depends on (all handed out earlier, to running CTAs)
+          const long long t0 = clock64();
+          while (ld_acquire_gpu(counters + w.wait) < w.need) {
+            if (*err || clock64() - t0 > spin_limit) {
+              if (atomicCAS(state + 1, 0, PGX_PERSIST_TIMEOUT) == 0) state[2] = it;
+              go = 0;
+              break;
+            }
+            __nanosleep(100);
+          }
+          __threadfence();  // the producers' results are read with plain loads from here on
+        }
+        if (go) next = atomicAdd(state, 1);
+      }
+      s_item = it;
+      s_go = go;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const pgx_persist_item w = items[s_item];
+    {
+      const double* src = reinterpret_cast<const double*>(descs + w.desc);
+      double* dst = reinterpret_cast<double*>(sI);
+      for (int i = threadIdx.x; i < (int)(sizeof(pgx_instance) / 8); i += blockDim.x) dst[i] = src[i];
+      // the program's header and the ops it uses (not all PGX_MAX_OPS)
+      const pgx_program* gp = progs + w.prog;
+      const int words = (int)((offsetof(pgx_program, ops) + sizeof(pgx_op) * (size_t)min(max(gp->nops, 0),
+                                                                                          PGX_MAX_OPS)) / 4);
+      const int* ps = reinterpret_cast<const int*>(gp);
+      int* pd = reinterpret_cast<int*>(sP);
+      for (int i = threadIdx.x; i < words; i += blockDim.x) pd[i] = ps[i];
+    }
+    __syncthreads();
+    run_program<true>(*sP, *sI, w.tile, slots);
+    // run_program ends every op with a block barrier: every store of the tile is done here
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(counters + w.done, 1);
+    }
+  }
 }
 
 // Two builds of the interpreter: with the FFT code (programs with DCT ops; up to 768 threads,
 // 80 registers a thread without spills) and without it (up to 1024 threads, 64 registers).
 __global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_single(const __grid_constant__ pgx_program P,
                                                                        const __grid_constant__ pgx_instance I) {
-  run_program<false, false>(P, I, blockIdx.x);
+  extern __shared__ __align__(16) double smem_dyn[];
+  run_program<false>(P, I, blockIdx.x, smem_dyn);
 }
 
 __global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_single_fft(const __grid_constant__ pgx_program P,
                                                                                const __grid_constant__ pgx_instance I) {
-  run_program<false, true>(P, I, blockIdx.x);
+  extern __shared__ __align__(16) double smem_dyn[];
+  run_program<true>(P, I, blockIdx.x, smem_dyn);
 }
 
 __global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_batched(const __grid_constant__ pgx_program P,
@@ -1263,9 +1635,9 @@ namespace pgx {
 // own thread): raise it once per device to the opt-in maximum -- it is only a
 // cap -- rather than track a per-thread high-water mark that another thread
 // could invalidate by setting a lower value.
-static int raise_smem_cap(const void* fn, int which) {
+static int raise_smem_cap_once(const void* fn, int which) {
   static std::mutex mu;
-  static bool done[4][64] = {};
+  static bool done[5][64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
@@ -1275,10 +1647,19 @@ static int raise_smem_cap(const void* fn, int which) {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return (int)e;
-  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, fn);
+  if (e != cudaSuccess) return (int)e;
+  // the cap covers dynamic shared memory; the kernel's static shared memory comes on top
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
   if (e != cudaSuccess) return (int)e;
   done[which][dev] = true;
   return 0;
+}
+static int raise_smem_cap(const void* fn, int which) {
+  const int e = raise_smem_cap_once(fn, which);
+  if (e) cudaGetLastError();  // a failed call leaves no pending error for the next launch to report
+  return e;
 }
 
 int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, int ntiles) {
@@ -1291,6 +1672,42 @@ int launch_single(const pgx_program* P, const pgx_instance* I, cudaStream_t s, i
   }
   if (fft) line_program_single_fft<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
   else line_program_single<<<ntiles, P->nthreads, smem, s>>>(*P, *I);
+  return (int)cudaGetLastError();
+}
+
+int persistent_shape(const pgx_program* progs, int nprogs, int threads, int* out_threads, int* ctas_per_sm,
+                     int64_t* smem) {
+  int64_t need = 0;
+  int nt = 32;
+  for (int i = 0; i < nprogs; ++i) {
+    const int64_t m = pgx_program_smem(progs + i);
+    if (m > need) need = m;
+    if (progs[i].nthreads > nt) nt = progs[i].nthreads;
+  }
+  if (threads > 0) nt = threads;
+  need += kPersistHead;
+  int e = raise_smem_cap((const void*)line_program_persistent, 4);
+  if (e) return e;
+  int per = 0;
+  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, line_program_persistent, nt, (size_t)need);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    return (int)ce;
+  }
+  *out_threads = nt;
+  *ctas_per_sm = per;
+  *smem = need;
+  return 0;
+}
+
+int launch_persistent(const pgx_program* d_progs, int nprogs, const pgx_instance* d_descs, int ndescs,
+                      const pgx_persist_item* d_items, int nitems, int32_t* d_counters, int ncounters,
+                      int32_t* d_state, int ctas, int threads, int64_t smem, long long spin_limit, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(d_counters, 0, sizeof(int32_t) * (size_t)ncounters, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_state, 0, 3 * sizeof(int32_t), s);
+  if (e != cudaSuccess) return (int)e;
+  line_program_persistent<<<ctas, threads, smem, s>>>(d_progs, nprogs, d_descs, ndescs, d_items, nitems, d_counters,
+                                                      ncounters, d_state, spin_limit);
   return (int)cudaGetLastError();
 }
 

@@ -1382,6 +1382,126 @@ class FusedBatch:
         for *_, st in self._pipe:
             main.wait_stream(st)
 
+    # ------------------------------------------------- persistent launch
+    def persistent(self, nsteps=1, threads=0, ctas=0, spin_seconds=1.0):
+        """Prepare ``nsteps`` steps of every instance as ONE launch (``pgx_run_persistent``).
+
+        The launches of the step become work items -- (program, descriptor, tile) of every pass,
+        size class and instance, step after step, pass after pass -- that the CTAs of one resident
+        grid take from a queue.  An item of pass p of instance k waits for instance k's pass p - 1
+        (pass 0 of a step for the previous step's last pass), so every instance runs through its
+        passes and steps at its own pace while others are still in earlier passes.  The programs
+        keep this batch's tiles; every one runs with the launch's CTA size (``threads``: 0 = the
+        largest of the programs').  ``ctas`` = 0: every CTA the device holds at once.  A wait that
+        lasts longer than ``spin_seconds`` ends the launch with an error (``persistent_error``)."""
+        lib = _lib.lib()
+        progs, desc_host, desc_base, per_pass = [], [], [], []
+        npass, ninst = len(self.launches), len(self.insts)
+        need = np.zeros((ninst, npass), dtype=np.int64)
+        ndesc = 0
+        for p, group in enumerate(self.launches):
+            host = getattr(group[0]["d_insts"], "pgx_host", None)
+            if host is None:
+                raise RuntimeError("%s: launch descriptors without their host copy" % group[0]["name"])
+            desc_host.append(host)
+            desc_base.append(ndesc)
+            ndesc += len(host)
+            its = []
+            for L in group:
+                if L["d_insts"] is not group[0]["d_insts"]:
+                    raise RuntimeError("%s: the size classes of a pass must share its descriptors" % L["name"])
+                nv = len(L["prog"].variants)
+                for d, t in L["d_work"].cpu().numpy().reshape(-1, 2):
+                    k = int(d) // nv
+                    its.append((len(progs), desc_base[p] + int(d), int(t), k))
+                    need[k, p] += 1
+                progs.append(L["P"])
+            per_pass.append(its)
+        items = persistent_items(per_pass, need, nsteps)
+        h_progs = (_lib.PgxProgram * len(progs))(*progs)
+        descs = (_lib.PgxInstance * ndesc)()
+        for host, base in zip(desc_host, desc_base):
+            ctypes.memmove(ctypes.addressof(descs) + base * ctypes.sizeof(_lib.PgxInstance), ctypes.addressof(host),
+                           ctypes.sizeof(host))
+        dev = device()
+        shape = (ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64())
+        _lib.check(lib.pgx_persistent_shape(ctypes.byref(h_progs), len(progs), int(threads),
+                                            *[ctypes.byref(x) for x in shape]), "persistent shape")
+        self._persist = {
+            "h_progs": h_progs, "nprogs": len(progs),
+            "d_progs": torch.frombuffer(bytearray(bytes(h_progs)), dtype=torch.uint8).to(dev),
+            "d_descs": torch.frombuffer(bytearray(bytes(descs)), dtype=torch.uint8).to(dev), "ndescs": ndesc,
+            "d_items": torch.as_tensor(np.asarray(items, dtype=np.int32).reshape(-1), device=dev),
+            "nitems": len(items), "ncounters": ninst * npass,
+            "d_counters": torch.zeros(ninst * npass, dtype=torch.int32, device=dev),
+            "d_state": torch.zeros(3, dtype=torch.int32, device=dev),
+            "ctas": int(ctas), "threads": int(shape[0].value), "ctas_per_sm": int(shape[1].value),
+            "smem": int(shape[2].value), "spin": int(spin_seconds * 2.1e9), "nsteps": nsteps,
+            "launch_generation": getattr(self, "launch_generation", 0), "graph": None}
+        return {k: self._persist[k] for k in ("nitems", "nprogs", "threads", "ctas_per_sm", "smem", "nsteps")}
+
+    def persistent_tiles(self, threads, ctas_per_sm):
+        """Re-pick every launch's tile for the persistent form: among the tiles the last ``autotune``
+        timed (alone), the fastest that runs with ``threads`` threads and leaves room for
+        ``ctas_per_sm`` CTAs of the persistent kernel on an SM (its descriptor and program head
+        included).  Launches without such a tile keep theirs.  Returns {"pass#group": tile}."""
+        lib = _lib.lib()
+        log = getattr(self, "tune_log", {})
+        cap = SMEM_PER_SM // ctas_per_sm - 1024 - PERSIST_HEAD
+        tiles = {}
+        for group in self.launches:
+            for gi, L in enumerate(group):
+                tag = "%s#%d" % (L["name"], gi)
+                for ms, tile in log.get(tag, []):
+                    if tile[1] != threads:
+                        continue
+                    P = self._group_launch(L["prog"], L["d_insts"], L["key"], L["members"], *tile[:3], L["name"],
+                                           *tile[3:5])["P"]
+                    if lib.pgx_program_smem(ctypes.byref(P)) <= cap:
+                        tiles[tag] = tuple(tile)
+                        break
+                else:
+                    tiles[tag] = (L["P"].tb, L["P"].nthreads, L["wc"], L["sd"], L["dm"])
+        self._build_launches(tiles)
+        return tiles
+
+    def run_persistent(self):
+        """Launch the persistent form prepared by ``persistent`` (``nsteps`` steps of every instance)."""
+        q = getattr(self, "_persist", None)
+        if q is None or q["launch_generation"] != getattr(self, "launch_generation", 0):
+            raise RuntimeError("persistent(): not prepared for the current launches")
+        _lib.check(_lib.lib().pgx_run_persistent(
+            ctypes.byref(q["h_progs"]), q["d_progs"].data_ptr(), q["nprogs"], q["d_descs"].data_ptr(), q["ndescs"],
+            q["d_items"].data_ptr(), q["nitems"], q["d_counters"].data_ptr(), q["ncounters"], q["d_state"].data_ptr(),
+            q["ctas"], q["threads"], q["spin"], stream()), "persistent step")
+
+    def capture_persistent(self):
+        """Record ``run_persistent`` (its counter resets and the one kernel) in a CUDA graph;
+        ``step_persistent`` replays it."""
+        q = self._persist
+        self.run_persistent()   # first launch outside the capture (kernel attributes)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run_persistent()
+        torch.cuda.synchronize()
+        q["graph"] = g
+
+    def step_persistent(self):
+        """``nsteps`` steps of every instance in one launch (graph replay once captured)."""
+        q = self._persist
+        if q["graph"] is not None:
+            q["graph"].replay()
+        else:
+            self.run_persistent()
+
+    def persistent_error(self):
+        """(error, item) of the last persistent launch: error 0 = every item ran (synchronises)."""
+        err, where = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(_lib.lib().pgx_persist_error(self._persist["d_state"].data_ptr(), ctypes.byref(err),
+                                                ctypes.byref(where), stream()), "persistent error")
+        return err.value, where.value
+
     def single(self, i):
         """Launch set of instance ``i`` alone (same tables and state): the one-by-one form."""
         one = FusedBatch.__new__(FusedBatch)
@@ -1469,6 +1589,34 @@ def program_work(prog, I):
         elif code in (_lib.OP["POISSON"], _lib.OP["POISSON_T"]):
             fl += 9.0 * slen[o.a] * lines
     return fl, by
+
+
+# bytes of a persistent CTA's shared memory before its slots: the descriptor and the program
+PERSIST_HEAD = 16 * (-(-ctypes.sizeof(_lib.PgxInstance) // 16) + -(-ctypes.sizeof(_lib.PgxProgram) // 16))
+
+
+def persistent_items(per_pass, need, nsteps):
+    """Work items of ``nsteps`` steps for ``pgx_run_persistent``: (prog, desc, tile, wait, need, done).
+
+    ``per_pass[p]`` lists the (prog, desc, tile, instance) items of pass p of one step and
+    ``need[k, p]`` how many of them belong to instance k.  Counter k * npass + p counts the completed
+    items of instance k's pass p over all steps of the launch.  The list runs step after step and
+    pass after pass, so an item always comes after every item it waits for: pass p of step s waits
+    for (s + 1) need[k, p - 1] completions of pass p - 1, pass 0 for s need[k, npass - 1] of the
+    last pass."""
+    npass = len(per_pass)
+    items = []
+    for st in range(nsteps):
+        for p in range(npass):
+            for prog, desc, tile, k in per_pass[p]:
+                if p > 0:
+                    wait, nd = k * npass + p - 1, (st + 1) * int(need[k, p - 1])
+                elif st > 0:
+                    wait, nd = k * npass + npass - 1, st * int(need[k, npass - 1])
+                else:
+                    wait, nd = -1, 0
+                items.append((prog, desc, tile, wait, nd, k * npass + p))
+    return items
 
 
 class FusedStep(FusedBatch):
