@@ -36,10 +36,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "2D RBC FP64 steps/s at 1 GB300: plain vs batched-graph; adjoint grads/s at 1e-6 rel"
-FP64_PEAK_TFLOPS = 1.256  # measured DFMA throughput of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt)
-# DRAM bytes (read + write) of pass P2 on the 256-instance workload, one ncu capture of its three size-class
-# launches (profiles/line_program_batched_c4_launches.txt)
-P2_DRAM_BYTES = 154.6e6 + 27.7e6
+# DFMA throughput of one GB300 at 2070 MHz measured with the same probe kernel (profiles/gb300_fp64_probe.txt);
+# used only when the in-process measurement (fp64_peak below) cannot run
+FP64_PEAK_FALLBACK_TFLOPS = 1.256
+# committed ncu summary of the dominant pass on the 256-instance workload: DRAM bytes per step of the pass
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "line_program_batched_c4_p2_traffic.txt")
 
 
 def workload_specs(kind, n_instances, rank=0):
@@ -148,6 +149,26 @@ class CpuPort:
             p.join()
 
 
+def cpu_sample(specs, steps, warmup):
+    """The one CPU measurement of both CPU legs (the GPU arm's ``cpu_baseline`` and the reference
+    arm): every instance of the workload in single-threaded spawned processes on all host cores,
+    ``warmup`` untimed steps, then ``steps`` timed steps.  Returns (instance-steps/s, cores,
+    description, wall s of the timed steps)."""
+    cores = min(host_cores(), len(specs))
+    port = CpuPort(specs, cores)
+    for _ in range(max(warmup, 1)):
+        port.step(1)
+    done, wall = 0, 0.0
+    for _ in range(steps):
+        d, w = port.step(1)
+        done, wall = done + d, wall + w
+    port.close()
+    desc = ("all %d instances x %d timed step(s) after %d warm-up, CPU oracle (%s) in %d single-threaded spawned "
+            "processes, %.1f s of stepping (%.0f core-s)"
+            % (len(specs), steps, max(warmup, 1), _oracle_flavour(), cores, wall, wall * cores))
+    return done / wall, cores, desc, wall
+
+
 def host_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -229,6 +250,80 @@ def time_steps(fn, steps, stream, between=None):
     return [a.elapsed_time(b) for a, b in ev]
 
 
+def fp64_peak(stream, reps=5):
+    """DFMA throughput of this GPU now (TFLOP/s): the library's FMA probe kernel on every SM
+    (4 CTAs x 256 threads each, 8 independent chains a thread), CUDA events on ``stream``, best
+    of ``reps`` launches of about 20 ms."""
+    import torch
+    from pypde_gb300 import _lib
+    L = _lib.lib()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    ctas, threads = 4 * sms, 256
+    out = torch.empty(ctas * threads, dtype=torch.float64, device="cuda")
+    iters = 4000
+    for _ in range(2):   # size the launch to about 20 ms
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _lib.check(L.pgx_fp64_fma_probe(out.data_ptr(), ctas, threads, iters, stream.cuda_stream), "fp64 probe")
+        b.record(stream)
+        torch.cuda.synchronize()
+        iters = max(1000, int(iters * 20.0 / max(a.elapsed_time(b), 1e-3)))
+    best = 0.0
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _lib.check(L.pgx_fp64_fma_probe(out.data_ptr(), ctas, threads, iters, stream.cuda_stream), "fp64 probe")
+        b.record(stream)
+        torch.cuda.synchronize()
+        best = max(best, L.pgx_fp64_fma_probe_flops(ctas, threads, iters) / (a.elapsed_time(b) * 1e-3) / 1e12)
+    return best
+
+
+def committed_traffic(pass_name, workload, n_inst):
+    """DRAM bytes (read + write) per step of ``pass_name`` from the committed ncu summary, with the
+    commit it was captured at, or (None, why)."""
+    if workload != "c4" or n_inst != 256:
+        return None, "no committed capture for this workload"
+    try:
+        fields = {}
+        for line in open(TRAFFIC_PROFILE):
+            if ":" in line and not line.startswith(" "):
+                k, v = line.split(":", 1)
+                fields[k.strip()] = v.strip()
+        if fields.get("pass") != pass_name:
+            return None, "the committed capture is of pass %s" % fields.get("pass")
+        return float(fields["dram_bytes_per_step"]), "%s (captured at commit %s)" % (
+            os.path.relpath(TRAFFIC_PROFILE, ROOT), fields.get("commit", "?"))
+    except (OSError, KeyError, ValueError) as e:
+        return None, "no committed capture (%s)" % e
+
+
+def batch_parity(fb, saved, specs, every=16, steps=5):
+    """The benched batch from its initial state, ``steps`` graph replays, against the CPU oracle on
+    every ``every``-th instance: max over instances and state arrays of max|gpu - oracle| / max|oracle|."""
+    import torch
+    from oracle import rbc2d as orb
+    fb.state_arena.copy_(saved)
+    for _ in range(steps):
+        fb.step()
+    torch.cuda.synchronize()
+    worst, checked = 0.0, 0
+    for i in range(0, len(specs), every):
+        shape, ra, dt, seed, amp, aspect = specs[i]
+        ref = orb.NavierStokes(case="linear", shape=shape, ra=ra, pr=1.0, dt=dt, aspect=aspect, dealias=True,
+                               integrator="eu", beta=1.0, tsave=None)
+        orb.seeded_temperature(ref, seed, amp)
+        for _ in range(steps):
+            ref.update()
+        st = fb.solvers[i].state()
+        for name, arr in (("T", ref.That), ("U", ref.Uhat), ("V", ref.Vhat), ("P", ref.Phat), ("pres", ref.pres)):
+            worst = max(worst, float(np.max(np.abs(st[name] - arr)) / max(np.max(np.abs(arr)), 1e-300)))
+        checked += 1
+    return {"max_rel_err": worst, "tolerance": 1e-8, "ok": worst < 1e-8, "instances_checked": checked,
+            "steps": steps, "how": "every %dth instance of the benched batch (its tuned tiles and graph), from the "
+                                   "initial state, against the CPU oracle" % every}
+
+
 def per_pass_times(fb, reps, stream, between=None):
     out = []
     for i in range(len(fb.launches)):
@@ -258,24 +353,13 @@ def run_gpu(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     specs = workload_specs(args.workload, args.instances, rank)
-    cores = host_cores()
 
     # CPU baseline first (spawned pool, before heavy GPU work), rank 0 only, N = 1 only
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        sample = specs[::8] if args.workload == "c4" else specs
-        ncores = min(cores, len(sample))
-        port = CpuPort(sample, ncores)
-        port.step(1)  # warm-up (first-step caches, BLAS initialisation)
-        done, wall, steps_cpu = 0, 0.0, 0
-        while wall < 10.0 and steps_cpu < 1000:  # a bounded sample: about 10 s of stepping
-            d, w = port.step(1)
-            done, wall, steps_cpu = done + d, wall + w, steps_cpu + 1
-        port.close()
-        cpu = {"value": done / wall, "unit": "instance-steps/s", "cores": ncores, "kind": "port", "blas_threads": 1,
-               "sample": "every 8th instance (%d of %d, same size / Ra mix) x %d step(s), CPU oracle (%s) "
-                         "in %d single-threaded processes, %.1f s of stepping"
-                         % (len(sample), len(specs), steps_cpu, _oracle_flavour(), ncores, wall)}
+        v, ncores, desc, _ = cpu_sample(specs, args.steps, args.warmup)
+        cpu = {"value": v, "unit": "instance-steps/s", "cores": ncores, "kind": "port", "blas_threads": 1,
+               "sample": desc}
 
     solvers, fb = build_batch(specs, {"auto": None, "on": True, "off": False}[args.split])
     n_inst = len(solvers)
@@ -301,6 +385,7 @@ def run_gpu(args, rank, world):
         if not args.no_graph_tiles:   # the dominant pass's tiles once more, inside the step's graph
             group_times["in_graph"] = {k: [list(v[0]), v[1]] for k, v in fb.tune_in_graph().items()}
     state_bytes = fb.state_arena.numel() * 8
+    initial_state = fb.state_arena.clone()   # tuning restores the state: this is the seeded initial state
     work_bytes = fb.scratch_bytes()
     flush, l2_note = l2_flusher(work_bytes)
 
@@ -350,28 +435,35 @@ def run_gpu(args, rank, world):
     if rank != 0:
         return None
 
-    # roofline of the dominant pass: algorithmic flops / CUDA-event time per launch
+    # the benched batch against the oracle: a fixed sample, from the initial state, tuned tiles and graph
+    parity = batch_parity(fb, initial_state, specs) if args.workload == "c4" else None
+
+    # roofline of the dominant pass: algorithmic flops / CUDA-event time per launch, against the DFMA
+    # throughput measured here, now (same process, same clocks)
     pt = per_pass_times(fb, 5, stream, flush)
+    try:
+        peak, peak_src = fp64_peak(stream), ("DFMA throughput measured in this run by the library's FMA probe "
+                                             "kernel (pgx_fp64_fma_probe, every SM); MEASURED_PEAKS.json "
+                                             "carries only HBM and bf16")
+    except Exception as e:  # pragma: no cover - probe missing from an old build
+        peak, peak_src = FP64_PEAK_FALLBACK_TFLOPS, "committed DFMA measurement at 2070 MHz (%s)" % e
     work = fb.pass_work()
     passes = []
     for (name, fl, by), ms in zip(work, pt):
         passes.append({"pass": name, "ms": round(ms, 4), "gflop": round(fl / 1e9, 4),
-                       "tflops": round(fl / (ms * 1e-3) / 1e12, 4), "frac_fp64": round(fl / (ms * 1e-3) / 1e12 /
-                                                                                         FP64_PEAK_TFLOPS, 4),
-                       "gb": round(by / 1e9, 5)})
+                       "frac_fp64": round(fl / (ms * 1e-3) / 1e12 / peak, 4)})
     dom = max(range(len(pt)), key=lambda i: pt[i])
     fl_dom = work[dom][1]
     achieved = fl_dom / (pt[dom] * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "kernel": "line_program_batched (%s)" % work[dom][0], "achieved": round(achieved, 4),
-                "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4),
-                "traffic": P2_DRAM_BYTES if (work[dom][0] == "P2" and args.workload == "c4" and n_inst == 256)
-                else None,
-                "peak_source": "measured DFMA peak of this GB300 at 2070 MHz (profiles/gb300_fp64_probe.txt, "
-                               "pypde_gb300/csrc/fp64_probe.cu); MEASURED_PEAKS.json carries only HBM and bf16",
-                "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2]}
+    traffic, traffic_src = committed_traffic(work[dom][0], args.workload, n_inst)
+    roofline = {"bound": "fp64", "kernel": "line_program_batched_fft (%s)" % work[dom][0],
+                "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": traffic_src,
+                "peak_source": peak_src, "flops_per_launch": fl_dom, "algorithmic_bytes_per_launch": work[dom][2],
+                "launch_ms": round(pt[dom], 4)}
     step_fl = sum(w[1] for w in work)
     step_fp64 = {"tflops": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12, 4),
-                 "frac": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12 / FP64_PEAK_TFLOPS, 4),
+                 "frac": round(step_fl / (total_ms / args.steps * 1e-3) / 1e12 / peak, 4),
                  "gflop_per_step": round(step_fl / 1e9, 3)}
 
     # one by one on the per-instance GPU path (same fused kernels, one CUDA graph per instance)
@@ -393,18 +485,21 @@ def run_gpu(args, rank, world):
     eager = None
     if not args.no_plain:
         sample = solvers[: min(8, n_inst)]
-        for ns in sample:
-            ns.update()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        for ns in sample:
-            for _ in range(2):
-                ns.update()
-        torch.cuda.synchronize()
-        dt_s = time.perf_counter() - t
-        eager = {"value": 2 * len(sample) / dt_s, "unit": "instance-steps/s",
-                 "how": "NavierStokes.update() op by op (plain drop-in path), %d instances x 2 steps, host "
-                        "wall clock" % len(sample)}
+        eager = {}
+        for label, fused in (("plain", False), ("default", None)):
+            for ns in sample:
+                ns.update(fused=fused)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for ns in sample:
+                for _ in range(2):
+                    ns.update(fused=fused)
+            torch.cuda.synchronize()
+            eager[label] = round(2 * len(sample) / (time.perf_counter() - t), 2)
+        eager.update({"unit": "instance-steps/s",
+                      "how": "NavierStokes.update() per call, %d instances x 2 steps, host wall clock: plain = "
+                             "update(fused=False), op by op; default = update(), the fused passes launched "
+                             "eagerly" % len(sample)})
 
     line = {
         "metric": METRIC,
@@ -428,21 +523,22 @@ def run_gpu(args, rank, world):
         "e2e": e2e,
         "gpu_launches": fb.graph_launches * args.steps,
         "roofline": roofline,
+        "parity": parity,
+        "clocks": clk,
+        "cpu_baseline": cpu,
         "step_fp64": step_fp64,
         "passes": passes,
         "plain": plain,
         "eager": eager,
-        "autotuned_tiles": tuned,
-        "graph_groups": {"groups": fb.graph_groups, "tuned_ms_per_step": group_times},
+        "graph_groups": {"groups": fb.graph_groups,
+                         "tuned_ms_per_step": {k: v for k, v in (group_times or {}).items() if k != "in_graph"}},
         "finite_instances": finite,
         "host_wall_s": round(wall, 3),
     }
-    if clk:
-        line["clocks"] = clk
-    if cpu:
-        line["cpu_baseline"] = cpu
     if world == 1 and args.adjoint_iters >= 0 and args.workload == "c4":
         line["adjoint"] = run_adjoint(args, stream)
+    # the long tables last: tiles of every launch
+    line["autotuned_tiles"] = {k: list(v[:5]) for k, v in tuned.items()} if isinstance(tuned, dict) else tuned
     return line
 
 
@@ -585,7 +681,8 @@ def dense_dct_passes(f, c, g, axis, mma, st):
 def run_microbench(args):
     """Kernel microbench (seed 1): DCT-I forward + backward along each axis of N x N fields,
     N = 33 ... 1025, and the ADI Helmholtz solve (I - 0.01 Laplacian) u = f with Dirichlet bases
-    at 257^2 and 1025^2; CUDA-event times, round-trip error against the input."""
+    at 257^2 and 1025^2, by the ADI plan and exactly by fast diagonalisation; CUDA-event times, round-trip
+    error against the input, residual of each solve's operator."""
     import torch
     import pypde_gb300 as pg
     from pypde_gb300 import _lib
@@ -626,19 +723,36 @@ def run_microbench(args):
                     "ms_fwd_bwd": round(t2, 5), "roundtrip_err": err2,
                     "tflops": round(2 * 2.0 * N * N * N / (t2 * 1e-3) / 1e12, 4)}
         dct.append(row)
-    hh = []
+    from oracle import spectral as sp
+    hh, hfd = [], []
     for N in (257, 1025):
         fld = pg.Field([pg.Base(N, "CD"), pg.Base(N, "CD")])
-        sol = pg.solverplan_hholtz2d_adi(fld.xs, lam=0.01)
-        f = torch.as_tensor(rng.uniform(-1, 1, (N, N)), device="cuda")
-        run = lambda: sol.solve_lhs(sol.solve_rhs(f))  # noqa: E731
-        for _ in range(3):
-            run()
-        ms = time_steps(run, max(args.steps, 5), stream, flush)
-        hh.append({"N": N, "ms": round(statistics.median(ms), 4), "launches": 4})
-    return {"metric": "kernel microbench: DCT-I fwd+bwd per axis and ADI Helmholtz solve", "dct": dct,
-            "helmholtz_adi": hh, "dtype": "f64", "data": "synthetic U(-1,1), seed 1",
-            "l2": "flushed between timed calls (a 258 MB write)"}
+        fh = rng.uniform(-1, 1, (N, N))
+        f = torch.as_tensor(fh, device="cuda")
+        S, B, I = sp.stencil("CD", N), sp.B2(N), sp.I2(N)
+        C, A = B @ S, I @ S
+        Bf = B @ fh @ B.T
+        for exact in (False, True):
+            sol = (pg.solverplan_hholtz2d_fd if exact else pg.solverplan_hholtz2d_adi)(fld.xs, lam=0.01)
+            run = lambda: sol.solve_lhs(sol.solve_rhs(f))  # noqa: E731
+            for _ in range(3):
+                x = run()
+            ms = time_steps(run, max(args.steps, 5), stream, flush)
+            x = x.cpu().numpy()
+            if exact:   # residual of the unsplit operator (C - lam A) X C^T - lam C X A^T = B F B^T
+                r = (C - 0.01 * A) @ x @ C.T - 0.01 * C @ x @ A.T - Bf
+                hfd.append({"N": N, "ms": round(statistics.median(ms), 4), "launches": 4,
+                            "residual": float(np.max(np.abs(r)) / np.max(np.abs(Bf)))})
+            else:       # residual of the ADI-factored system A_x X A_y^T = B F B^T, A = C - lam I S
+                Ax = C - 0.01 * A
+                r = Ax @ x @ Ax.T - Bf
+                hh.append({"N": N, "ms": round(statistics.median(ms), 4), "launches": 4,
+                           "residual": float(np.max(np.abs(r)) / np.max(np.abs(Bf)))})
+    return {"metric": "kernel microbench: DCT-I fwd+bwd per axis and Helmholtz solves", "dct": dct,
+            "helmholtz_adi": hh, "helmholtz_exact_fd": hfd, "dtype": "f64", "data": "synthetic U(-1,1), seed 1",
+            "l2": "flushed between timed calls (a 258 MB write)",
+            "residual": "max |operator(x) - B F B^T| / max |B F B^T| with the premultiplied operator of each plan "
+                        "(ADI: its factored operator; exact: the unsplit one, bounded by the host eigendecomposition)"}
 
 
 def run_reference(args, rank, world):
@@ -648,30 +762,14 @@ def run_reference(args, rank, world):
         return None
     specs = workload_specs(args.workload, args.instances)
     full = len(specs)
-    if args.workload == "c4":
-        specs = specs[::4]  # a bounded sample with the same size / Ra mix
-    cores = min(host_cores(), len(specs))
-    port = CpuPort(specs, cores)
-    for _ in range(max(args.warmup, 1)):
-        port.step(1)
-    total_done, total_wall = 0, 0.0
-    for _ in range(args.steps):
-        done, wall = port.step(1)
-        total_done += done
-        total_wall += wall
-    port.close()
-    value = total_done / total_wall
+    value, cores, desc, total_wall = cpu_sample(specs, args.steps, args.warmup)
     return {"metric": METRIC, "value": round(value, 3), "unit": "instance-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded U(-1,1) temperature noise (seeds 100+i)", "impl": "reference",
             "config": {"workload": WORKLOAD_NAMES[args.workload].format(n=full), "instances_per_gpu": full},
             "cpu_baseline": {"value": round(value, 3), "unit": "instance-steps/s", "cores": cores, "kind": "port",
-                             "blas_threads": 1,
-                             "sample": "every %s instance (%d of %d, same size / Ra mix), 1 step per timed step, "
-                                       "%d single-threaded spawned processes running the CPU oracle (%s)"
-                                       % ("4th" if full != len(specs) else "", len(specs), full, cores,
-                                          _oracle_flavour())},
+                             "blas_threads": 1, "sample": desc},
             "e2e": {"value": round(value, 3), "unit": "instance-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
