@@ -1372,7 +1372,10 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int n = c.slen[op.a];
   if (((n - 1) & 1) == 0 && n >= 3) {
-    if (op.k & PGX_DCT_CTA) op_dct_even_cta(c, op, I);
+    // a tile with fewer line pairs per slot than warps (single instances, short passes) leaves
+    // warps idle in the warp-local form; there the CTA-wide form spreads each pair over all warps
+    // (per slot, so a multi-slot op and its one-op-per-slot split take the same form)
+    if ((op.k & PGX_DCT_CTA) || ((c.tb + 1) >> 1) < (c.nthreads >> 5)) op_dct_even_cta(c, op, I);
     else op_dct_even(c, op, I);
     return;
   }
