@@ -11,7 +11,9 @@ graph of eleven fused line-program launches.  ``value`` = instance-steps/s with
 the state resident in HBM; ``e2e`` = the same through the public API with the
 state in pinned host memory (one H2D copy of every instance's state before and
 one D2H copy after each step, inside the timed region).  ``plain`` = the same
-instances run one by one on the per-instance GPU path.  ``adjoint`` = the
+instances run one by one on the per-instance GPU path.  ``persistent`` = the
+same batch with several steps of every instance in one persistent launch
+(pgx_run_persistent), replayed from a graph.  ``adjoint`` = the
 adjoint steady-state search (129 x 129, Ra 1e5, 200-step horizon, checkpoints
 every 20 steps): gradients/s, cost against the forward sweep, finite-difference
 check on 20 random directions, 50 descent iterations.
@@ -501,6 +503,29 @@ def run_gpu(args, rank, world):
                              "update(fused=False), op by op; default = update(), the fused passes launched "
                              "eagerly" % len(sample)})
 
+    # the same batch as persistent launches (several steps of every instance in one launch of a resident
+    # grid, tiles re-picked for one CTA size), recorded in a CUDA graph
+    persistent = None
+    if args.workload == "c4" and n_inst > 1 and args.persistent_steps > 0:
+        T, per_sm, K = 128, 6, args.persistent_steps
+        fb.persistent_tiles(T, per_sm)
+        fb.state_arena.copy_(initial_state)
+        info = fb.persistent(nsteps=K, threads=T)
+        fb.capture_persistent()
+        for _ in range(2):
+            fb.step_persistent()
+        torch.cuda.synchronize()
+        reps = max(1, args.steps // K)
+        ms = time_steps(fb.step_persistent, reps, stream, flush)
+        err, where = fb.persistent_error()
+        persistent = {"value": round(n_inst * K * reps / (sum(ms) / 1e3), 2), "unit": "instance-steps/s",
+                      "ms_per_step": round(sum(ms) / (reps * K), 4), "steps_per_launch": K, "launches": reps,
+                      "threads": info["threads"], "ctas_per_sm": info["ctas_per_sm"], "items_per_launch": info["nitems"],
+                      "error": err,
+                      "how": "pgx_run_persistent: %d steps of all %d instances per launch (work queue, per-instance "
+                             "pass counters), tiles re-picked from the autotuner's timings for %d-thread CTAs, "
+                             "%d per SM; one CUDA-graph replay per launch" % (K, n_inst, T, per_sm)}
+
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -529,6 +554,7 @@ def run_gpu(args, rank, world):
         "step_fp64": step_fp64,
         "passes": passes,
         "plain": plain,
+        "persistent": persistent,
         "eager": eager,
         "graph_groups": {"groups": fb.graph_groups,
                          "tuned_ms_per_step": {k: v for k, v in (group_times or {}).items() if k != "in_graph"}},
@@ -785,6 +811,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--persistent-steps", type=int, default=4,
+                    help="c4: steps per launch of the persistent form measured beside the graph form (0: skip)")
     ap.add_argument("--tiles", default=None, help="use the tiles saved by --save-tiles instead of tuning")
     ap.add_argument("--adjoint-groups", type=int, default=1,
                     help="instance groups of the batched gradient, each on its own stream (measured on the "
