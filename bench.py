@@ -556,8 +556,7 @@ def run_gpu(args, rank, world):
         "plain": plain,
         "persistent": persistent,
         "eager": eager,
-        "graph_groups": {"groups": fb.graph_groups,
-                         "tuned_ms_per_step": {k: v for k, v in (group_times or {}).items() if k != "in_graph"}},
+        "graph_groups": {"groups": fb.graph_groups, "tuned_ms_per_step": group_times},
         "finite_instances": finite,
         "host_wall_s": round(wall, 3),
     }
