@@ -386,6 +386,8 @@ def run_gpu(args, rank, world):
         group_times = {str(k): round(v, 4) for k, v in fb.tune_groups().items()}
         if not args.no_graph_tiles:   # the dominant pass's tiles once more, inside the step's graph
             group_times["in_graph"] = {k: [list(v[0]), v[1]] for k, v in fb.tune_in_graph().items()}
+        # the fastest of a few recordings of the final graph (the same launches and branches)
+        group_times["recordings"] = [round(t, 4) for t in fb.capture_best()]
     state_bytes = fb.state_arena.numel() * 8
     initial_state = fb.state_arena.clone()   # tuning restores the state: this is the seeded initial state
     work_bytes = fb.scratch_bytes()

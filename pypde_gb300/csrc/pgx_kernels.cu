@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "pgx.h"
+#include "pgx_exact.cuh"
 
 // Complex elements per line pair in each FFT buffer for DCT lengths up to n:
 // n - 1 for the folded algorithm (even n - 1), 2(n - 1) for paired lines.
@@ -789,6 +790,16 @@ struct DctScale {
       default: return 1.0;
     }
   }
+  // u * pre(j, N), bit for bit; the +-1/2 and 1 of BWD and BWD_T on the bit pattern (no FP64 instruction)
+  __device__ __forceinline__ double scale_pre(double u, int j, int N) const {
+    const bool end = (j == 0 || j == N);
+    switch (mode) {
+      case PGX_DCT_BWD: return end ? ((j & 1) ? -u : u) : pgx_half_signed(u, (j & 1) != 0);
+      case PGX_DCT_BWD_T: return end ? u : pgx_half_signed(u, false);
+      case PGX_DCT_FWD_T: return u * pre(j, N);
+      default: return u;
+    }
+  }
   __device__ __forceinline__ double post(int k, int N) const {
     const bool end = (k == 0 || k == N);
     const double sg = (k & 1) ? -1.0 : 1.0;
@@ -835,9 +846,8 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
         double a = x[t0 * c.lcap + sidx];
         double b = two ? x[(t0 + 1) * c.lcap + sidx] : 0.0;
         if (ds.has_pre) {
-          const double w = ds.pre(sidx, N);
-          a *= w;
-          b *= w;
+          a = ds.scale_pre(a, sidx, N);
+          b = ds.scale_pre(b, sidx, N);
         }
         v[r] = make_double2(a, b);
       } else {
@@ -952,9 +962,8 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
         ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
       }
       if (ds.has_pre) {
-        const double sg = ds.pre(m, N);
-        ua *= sg;
-        ub *= sg;
+        ua = ds.scale_pre(ua, m, N);
+        ub = ds.scale_pre(ub, m, N);
       }
       v[r] = make_double2(ua, ub);
     }
@@ -1192,9 +1201,8 @@ __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2*
         ub = fma(cm, b0 - b1, b1);
       }
       if (ds.has_pre) {
-        const double sg = ds.pre(m, N);
-        ua *= sg;
-        ub *= sg;
+        ua = ds.scale_pre(ua, m, N);
+        ub = ds.scale_pre(ub, m, N);
       }
       v[r] = make_double2(ua, ub);
     }

@@ -1285,6 +1285,33 @@ class FusedBatch:
         self.graph_launches = sum(sub.launches_per_step for sub, _ in branches) if len(branches) > 1 \
             else self.launches_per_step
 
+    def capture_best(self, tries=4, reps=10):
+        """Record the step's graph ``tries`` times (same launches and branches as the last ``capture``)
+        and keep the recording whose replays run fastest: replays of graphs with several parallel
+        branches differ by a few percent from one recording to the next.  The state is restored
+        after every trial.  Returns the ms per step of every recording."""
+        groups = getattr(self, "graph_groups_arg", 1)
+        saved = self.state_arena.clone()
+        best, times = None, []
+        for _ in range(tries):
+            self.capture(1, groups=groups)
+            for _ in range(3):
+                self.step()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for a, b in ev:
+                a.record()
+                self.step()
+                b.record()
+            torch.cuda.synchronize()
+            times.append(sum(a.elapsed_time(b) for a, b in ev) / reps)
+            self.state_arena.copy_(saved)
+            if best is None or times[-1] < best[0]:
+                best = (times[-1], self.graph, self.graph_branches, self.graph_groups, self.graph_launches)
+        _, self.graph, self.graph_branches, self.graph_groups, self.graph_launches = best
+        self.graph_steps = 1
+        torch.cuda.synchronize()
+        return times
+
     def step(self):
         """One fused step (graph replay when captured with nsteps == 1)."""
         if self.graph is not None and self.graph_steps == 1:

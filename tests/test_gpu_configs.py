@@ -117,6 +117,7 @@ def test_benchmark_batch_slice_tuned_graph_vs_oracle(torch):
     fb = FusedBatch(solvers)
     fb.autotune(reps=1)
     fb.tune_groups(reps=3)
+    assert len(fb.capture_best(tries=2, reps=2)) == 2   # the kept recording is the one stepped below
     assert fb.graph is not None
     for _ in range(5):
         fb.step()
