@@ -564,8 +564,14 @@ def run_gpu(args, rank, world):
     }
     if world == 1 and args.adjoint_iters >= 0 and args.workload == "c4":
         line["adjoint"] = run_adjoint(args, stream)
-    # the long tables last: tiles of every launch
     line["autotuned_tiles"] = {k: list(v[:5]) for k, v in tuned.items()} if isinstance(tuned, dict) else tuned
+    # the per-pass fractions and the parity check also inside roofline (a key every reader parses), and in
+    # full at the end of the line (the part of a long output that is kept when only its tail is)
+    roofline["passes_frac_fp64"] = {p["pass"]: p["frac_fp64"] for p in passes}
+    if parity is not None:
+        roofline["parity_max_rel_err"] = parity["max_rel_err"]
+    for k in ("step_fp64", "parity", "passes"):
+        line[k] = line.pop(k)
     return line
 
 
