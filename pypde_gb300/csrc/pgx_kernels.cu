@@ -47,6 +47,15 @@ __host__ __device__ inline int pgx_fft_slots(const pgx_program& P) {
   return fs;
 }
 
+// A program whose DCT ops each transform one slot, tiled in pairs of lines, with the folded transform
+// (even n - 1: a pair's FFT data takes n - 1 complex values, at most its two lines of the slot) keeps
+// its second FFT buffer in the spare slot: nothing lives there during a DCT op, and every op that
+// later writes the spare overwrites or zeroes all of it.  One buffer less of shared memory per CTA.
+__host__ __device__ inline bool pgx_fft_in_spare(const pgx_program& P) {
+  if (P.fft_n <= 1 || pgx_fft_slots(P) != 1 || (P.tb & 1)) return false;
+  return 2LL * pgx_fft_stride(P.fft_n) * ((P.tb + 1) / 2) <= (long long)P.tb * P.lcap;
+}
+
 namespace pgx {
 
 // 2k for k < PGX_LMAX: multipliers of the derivative recurrence, read through
@@ -1461,9 +1470,10 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   size_t off = (size_t)nbuf * c.tb * c.lcap;
   c.fft_stride = pgx_fft_stride(P.fft_n);
   const int fs = pgx_fft_slots(P);
+  const bool fft_in_spare = FFT && pgx_fft_in_spare(P);
   c.f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
-  c.f1 = c.f0 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride;
-  c.ybuf = reinterpret_cast<double*>(c.f1 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride);
+  c.f1 = fft_in_spare ? nullptr : c.f0 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride;
+  c.ybuf = reinterpret_cast<double*>((fft_in_spare ? c.f0 : c.f1) + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride);
   for (int s = 0; s < nbuf; ++s) c.phys[s] = s;
   for (int s = 0; s < PGX_MAX_SLOTS; ++s) c.slen[s] = 0;
   c.spare = P.nslots;
@@ -1490,7 +1500,10 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
       case PGX_OP_TDMA2: op_tdma2(c, op, I); break;
       case PGX_OP_DIFF: op_diff(c, op); break;
       case PGX_OP_DCT:
-        if (FFT) op_dct(c, op, I);  // programs with DCT ops run the FFT kernels only
+        if (FFT) {  // programs with DCT ops run the FFT kernels only
+          if (fft_in_spare) c.f1 = reinterpret_cast<double2*>(spare_ptr(c));  // even tb: 16-byte aligned
+          op_dct(c, op, I);
+        }
         break;
       case PGX_OP_BANDED: op_banded(c, op, I); break;
       case PGX_OP_DENSE: op_dense(c, op, I); break;
@@ -1636,7 +1649,8 @@ extern "C" int64_t pgx_program_smem(const pgx_program* P) {
   int64_t doubles = nbuf * P->tb * P->lcap;
   doubles += doubles & 1;
   const int64_t fs = pgx_fft_slots(*P);
-  if (P->fft_n > 1) doubles += 2 * 2 * fs * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + fs * P->tb + 1;
+  const int64_t nbufs = pgx_fft_in_spare(*P) ? 1 : 2;  // the second FFT buffer may live in the spare slot
+  if (P->fft_n > 1) doubles += nbufs * 2 * fs * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + fs * P->tb + 1;
   return doubles * 8;
 }
 

@@ -835,13 +835,16 @@ CHAIN_OPS = ("FDMA", "POISSON", "TDMA2", "FDMA_T", "POISSON_T")
 _CHAIN_CODES = tuple(_lib.OP[k] for k in CHAIN_OPS)
 
 
-def fft_bytes_per_line(fft_n):
+def fft_bytes_per_line(fft_n, one_slot=False):
     """Shared memory of the DCT-I work buffers per line: two buffers of n-1 (folded algorithm,
-    even n-1) or 2(n-1) (paired lines) complex values per pair of lines, plus one scalar."""
+    even n-1) or 2(n-1) (paired lines) complex values per pair of lines, plus one scalar.  With
+    ``one_slot`` (every DCT op transforms one slot) and the folded algorithm the second buffer is
+    the spare slot (for an even number of lines per tile)."""
     if fft_n <= 1:
         return 0
-    stride = fft_n - 1 if (fft_n - 1) % 2 == 0 else 2 * (fft_n - 1)
-    return 16 * stride + 8
+    even = (fft_n - 1) % 2 == 0
+    stride = fft_n - 1 if even else 2 * (fft_n - 1)
+    return (8 if (one_slot and even) else 16) * stride + 8
 SMEM_PER_SM = 227 * 1024
 
 
@@ -869,7 +872,8 @@ def _pick(prog, lines_total, lcap, fft_n, max_lines):
     """
     nbuf = prog.nslots + 1
     sd = _fft_slots(prog) > 1 and fft_n > JOINT_DCT_MAX_N
-    per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
+    fs = _fft_slots(prog, sd)
+    per_line = 8 * nbuf * lcap + fs * fft_bytes_per_line(fft_n, fs == 1)
     chains = any(o.code in [_lib.OP[k] for k in CHAIN_OPS] for o in prog.ops)
     if fft_n > 1:
         budget = SMEM_PER_SM // 2 - 2048
@@ -929,7 +933,8 @@ def _has_dense(prog, fft_n):
 def _candidates_sd(prog, lines_total, lcap, fft_n, max_lines, sd, dm):
     ntmax = _max_threads(prog, fft_n, dm)
     nbuf = prog.nslots + 1
-    per_line = 8 * nbuf * lcap + _fft_slots(prog, sd) * fft_bytes_per_line(fft_n)
+    fs = _fft_slots(prog, sd)
+    per_line = 8 * nbuf * lcap + fs * fft_bytes_per_line(fft_n, fs == 1)
     width = 1
     for o in prog.ops:
         if o.code in _CHAIN_CODES:
