@@ -343,7 +343,9 @@ int pgx_matrix_apply(const pgx_matrix_plan* plan, const double* in, int64_t in_s
 int pgx_matrix_plan_is_banded(const pgx_matrix_plan* plan);
 
 /* Device tables for line programs built by the host: twiddle factors of the
- * DCT-I of n points, and the stencil sub-diagonal table.  The returned device
+ * DCT-I of n points (2(n-1) complex values exp(-2 pi i k / (2(n-1))), then the
+ * n-1 doubles 0.5 + Im(tw[m]) = 1/2 - sin(pi m / (n-1)) of the folded transform),
+ * and the stencil sub-diagonal table.  The returned device
  * pointer is owned by the library and valid until process exit. */
 int pgx_dct_table(int32_t n, const double** table);
 

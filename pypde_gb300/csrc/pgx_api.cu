@@ -260,7 +260,7 @@ bool fft_length_ok(int L) {
   return L == 1;
 }
 
-// key (device, n) -> twiddles exp(-2 pi i k / L), L = 2(n-1)
+// key (device, n) -> twiddles exp(-2 pi i k / L), L = 2(n-1), and the fold coefficients
 std::map<std::pair<int, int>, double*> g_tw;
 // key (device, n, mode) -> dense scaled cosine matrix for lengths the FFT does not cover
 std::map<std::pair<int, int>, double*> g_dense;
@@ -281,7 +281,9 @@ int twiddles(int n, const double** out) {
     *out = it->second;
     return PGX_OK;
   }
-  std::vector<double> h(2 * (size_t)L);
+  // L complex twiddles, then the fold coefficients 1/2 - sin(pi m / N) (m < N = L/2), each the
+  // FP64 sum 0.5 + Im(tw[m]) that the kernels would otherwise form per point
+  std::vector<double> h(2 * (size_t)L + L / 2);
   const double pi = 3.14159265358979323846;
   for (int k = 0; k < L; ++k) {
     double a = 2.0 * pi * (double)k / (double)L;
@@ -297,6 +299,7 @@ int twiddles(int n, const double** out) {
       h[2 * k + 1] = -sn[q];
     }
   }
+  for (int m = 0; m < L / 2; ++m) h[2 * (size_t)L + m] = 0.5 + h[2 * m + 1];
   double* d = nullptr;
   int rc = upload(h, &d);
   if (rc) return rc;

@@ -765,7 +765,8 @@ __device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 // DCT-I of two real lines at once: the even extensions e, e' (length L = 2(n-1))
 // form z = e + i e'; its DFT Z is y + i y' because the DFT of a real even
 // sequence is real.  The complex DFT is a mixed-radix (4, 2, 3) Stockham FFT in
-// shared memory; tw[k] = exp(-2 pi i k / L) comes from a host-built table.
+// shared memory; tw[k] = exp(-2 pi i k / L) comes from a host-built table (followed, for the folded
+// even transform, by the fold coefficients 1/2 - sin(pi m / N), m < N = L / 2).
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
@@ -945,13 +946,60 @@ __device__ __forceinline__ void stage_dispatch(int R, const Ctx& c, const double
   else stockham_stage<3, FIRST, LAST>(c, src, dst, tw, L, Ns, npairs, x, ds, tws);
 }
 
+// Radix plan of the length-N FFT: every factor 3 first (the first stage has no twiddles, and a
+// twiddled radix-3 stage costs the most FP64 instructions per point), then 4s, then one 2.
+struct RadixPlan {
+  int n3, n4, n2;  // stages of radix 3, then 4, then 2
+  __device__ __forceinline__ int stages() const { return n3 + n4 + n2; }
+  __device__ __forceinline__ int at(int s) const { return s < n3 ? 3 : (s < n3 + n4 ? 4 : 2); }
+};
+__device__ __forceinline__ RadixPlan radix_plan(int N, int& rest, bool radix2 = false) {
+  RadixPlan p{0, 0, 0};
+  int m = N;
+  while (m % 3 == 0) { ++p.n3; m /= 3; }
+  if (radix2) {
+    while (m % 2 == 0) { ++p.n2; m /= 2; }
+  } else {
+    while (m % 4 == 0) { ++p.n4; m /= 4; }
+    if (m % 2 == 0) { ++p.n2; m /= 2; }
+  }
+  rest = m;  // 1 for every length with a twiddle table (n - 1 = 2^a 3^b)
+  return p;
+}
+
+// Untwiddled radix-R butterfly (the first stage of an FFT).
+template <int R>
+__device__ __forceinline__ void butterfly_plain(double2* v, double2* o) {
+  if (R == 2) {
+    o[0] = cadd(v[0], v[1]);
+    o[1] = csub(v[0], v[1]);
+  } else if (R == 4) {
+    double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
+    o[0] = cadd(a, e);
+    o[2] = csub(a, e);
+    o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
+    o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
+  } else {  // R == 3, W3 = -1/2 - i sqrt(3)/2
+    const double h = 0.86602540378443864676;
+    double2 t1 = cadd(v[1], v[2]);
+    double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
+    double2 t3 = csub(v[1], v[2]);
+    o[0] = cadd(v[0], t1);
+    o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));  // t2 - i h t3
+    o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));  // t2 + i h t3
+  }
+}
+
 // The first radix-R stage of the even DCT's FFT (Ns = 1, no twiddles) with the fold computed on
-// its way in: u_m = (x_m + x_{N-m})/2 - sin(pi m/N) (x_m - x_{N-m}) of both lines of every pair,
-// read straight from the slots (no separate fold phase, one barrier fewer per transform).
+// its way in: u_m = (x_m + x_{N-m})/2 - sin(pi m/N) (x_m - x_{N-m}) = x_{N-m} + (1/2 - sin(pi m/N))
+// (x_m - x_{N-m}), one FMA a point, of both lines of every pair, read straight from the slots (no
+// separate fold phase, one barrier fewer per transform).
 template <int R>
 __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const double2* tw, int N, int nall,
                                            int npairs, int slot0, const DctScale& ds) {
   const int LR = N / R;
+  const double* cmt = reinterpret_cast<const double*>(tw + 2 * N);
   for (int idx = c.tid; idx < nall * LR; idx += c.nthreads) {
     const int P = idx / LR, j = idx - P * LR;
     const int sl = P / npairs, pr = P - sl * npairs;
@@ -962,13 +1010,13 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int m = j + r * LR;
-      const double sn = -__ldg(&tw[m].y);
+      const double cm = __ldg(cmt + m);  // 1/2 - sin(pi m / N), after the 2N twiddles
       const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
-      double ua = fma(-sn, a0 - a1, 0.5 * (a0 + a1));
+      double ua = fma(cm, a0 - a1, a1);
       double ub = 0.0;
       if (two) {
         const double b0 = x[(t0 + 1) * c.lcap + m], b1 = x[(t0 + 1) * c.lcap + N - m];
-        ub = fma(-sn, b0 - b1, 0.5 * (b0 + b1));
+        ub = fma(cm, b0 - b1, b1);
       }
       if (ds.has_pre) {
         ua = ds.scale_pre(ua, m, N);
@@ -977,25 +1025,7 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
       v[r] = make_double2(ua, ub);
     }
     double2 o[R];
-    if (R == 2) {
-      o[0] = cadd(v[0], v[1]);
-      o[1] = csub(v[0], v[1]);
-    } else if (R == 4) {
-      double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-      double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
-      o[0] = cadd(a, e);
-      o[2] = csub(a, e);
-      o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
-      o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
-    } else {  // R == 3
-      const double h = 0.86602540378443864676;
-      double2 t1 = cadd(v[1], v[2]);
-      double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
-      double2 t3 = csub(v[1], v[2]);
-      o[0] = cadd(v[0], t1);
-      o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));
-      o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));
-    }
+    butterfly_plain<R>(v, o);
 #pragma unroll
     for (int q = 0; q < R; ++q) dst[P * c.fft_stride + j * R + q] = o[q];
   }
@@ -1008,7 +1038,9 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
 //   FFT    Z = DFT_N(u_a + i u_b) for the two lines (a, b) of a pair
 //   untangle  y_{2m} = Z_m + conj(Z_{N-m}) (real / imag part for line a / b),
 //          odd increments y_{2m+1} - y_{2m-1} = Im(Z_{N-m} - Z_m) (a), Re(Z_m - Z_{N-m}) (b)
-//   scan   y_{2m+1} = y_1 + sum of increments (one warp per line).
+//   scan   y_{2m+1} = y_1 + sum of increments.
+// Every phase runs over all threads of the CTA (a barrier between phases), with the FFT's radix
+// plan (radix_plan), the fold and the per-line phases (L lanes a line) of the warp-local form.
 // tw is the table exp(-2 pi i k / (2N)): W_N^k = tw[2k], (cos, -sin)(pi j / N) = tw[j].
 // The backward pre-scale (-1)^j w_j is common to x_j and x_{N-j} (N even) and
 // applied to u_j, d_j; the forward post-scale to the outputs.
@@ -1023,47 +1055,49 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   const int npairs = (c.tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
-  if (N > c.fft_stride) {  // FFT buffers sized for a shorter length: refuse loudly
+  int rest = 1;
+  const RadixPlan plan = radix_plan(N, rest);
+  if (N > c.fft_stride || rest != 1 || plan.stages() < 1) {  // no buffer or plan for this length: refuse loudly
     for (int sl = 0; sl < ns; ++sl)
       for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
     return;
   }
-  // y_1: one warp per line (line lt = sl * tb + t)
+  // y_1, L lanes a line, the op's lines spread over the warps (line lt = sl * tb + t); the j of a
+  // lane keep one parity (L even), so the alternating pre-scale of BWD / FWD_T is one sign per lane
+  const int nlines = ns * c.tb;
+  const LineLanes g = line_lanes(c, nlines);
   {
-    const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
     const bool alt = mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T;
     const double ps = ds.has_pre ? (alt ? -ds.pre(1, N) : ds.pre(1, N)) : 1.0;
-    for (int lt = warp; lt < ns * c.tb; lt += nw) {
-      const int sl = lt / c.tb, t = lt - sl * c.tb;
+    const double p0 = ds.has_pre ? ds.pre(0, N) : 1.0;
+    for (int base = g.first; base < nlines; base += g.stride) {
+      const int lt = base + g.grp;
+      const bool valid = lt < nlines;
+      const int sl = valid ? lt / c.tb : 0, t = valid ? lt - sl * c.tb : 0;
       const double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
-      // the interior pre-scale is ps (-1)^j (alt) or ps: the sign is fixed per lane (j = 1 + lane
-      // mod 32), the magnitude applied once
       double acc = 0.0;
-      for (int j = 1 + lane; j < H; j += 32) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
-      if (alt && ((1 + lane) & 1)) acc = -acc;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      const double d0 = (xl[0] - xl[N]) * (ds.has_pre ? ds.pre(0, N) : 1.0);
-      if (lane == 0) c.ybuf[lt] = fma(2.0 * ps, acc, d0);
+      if (valid)
+        for (int j = 1 + g.sub; j < H; j += g.L) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
+      if (alt && ((1 + g.sub) & 1)) acc = -acc;
+      for (int o = g.L >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, g.L);
+      if (valid && g.sub == 0) c.ybuf[lt] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
     }
   }
-  // FFT of length N over all pairs (y_1 above and the first stage both only read the slots)
+  // FFT of length N over all pairs, the radix plan of the warp-local form (y_1 above and the first
+  // stage both only read the slots)
   double2* bufs[2] = {c.f0, c.f1};
-  int cur = 0, Ns = 1;
-  for (int rem = N; rem > 1;) {
-    const int R = next_radix(rem);
-    if (Ns == 1) {  // the fold on the way into the first stage
-      if (R == 4) fold_stage<4>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
-      else if (R == 2) fold_stage<2>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
-      else fold_stage<3>(c, bufs[cur ^ 1], tw, N, nall, npairs, op.a, ds);
-    } else {
-      stage_dispatch<false, false>(R, c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, nall, nullptr, ds, 2);
-    }
-    cur ^= 1;
-    Ns *= R;
-    rem /= R;
+  const int R0 = plan.at(0);
+  if (R0 == 3) fold_stage<3>(c, bufs[1], tw, N, nall, npairs, op.a, ds);
+  else if (R0 == 4) fold_stage<4>(c, bufs[1], tw, N, nall, npairs, op.a, ds);
+  else fold_stage<2>(c, bufs[1], tw, N, nall, npairs, op.a, ds);
+  int cur = 1, Ns = R0;
+  for (int s = 1; s < plan.stages(); ++s) {
     __syncthreads();
+    stage_dispatch<false, false>(plan.at(s), c, bufs[cur], bufs[cur ^ 1], tw, N, Ns, nall, nullptr, ds, 2);
+    cur ^= 1;
+    Ns *= plan.at(s);
   }
+  __syncthreads();
   const double2* Z = bufs[cur];
   // untangle: even outputs, odd increments
   for (int idx = c.tid; idx < nall * (H + 1); idx += c.nthreads) {
@@ -1091,23 +1125,25 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
     }
   }
   __syncthreads();
-  // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1 (one warp per line)
+  // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1, L lanes a line
   {
-    const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
-    const int chunk = (H + 31) / 32;
+    const int chunk = (H + g.L - 1) / g.L;
     const double osc = ds.has_post ? ds.post(1, N) : 1.0;  // the same for every odd k < N
-    for (int lt = warp; lt < ns * c.tb; lt += nw) {
-      const int sl = lt / c.tb, t = lt - sl * c.tb;
+    for (int base = g.first; base < nlines; base += g.stride) {
+      const int lt = base + g.grp;
+      const bool valid = lt < nlines;
+      const int sl = valid ? lt / c.tb : 0, t = valid ? lt - sl * c.tb : 0;
       double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
-      const int m0 = lane * chunk, m1 = min(m0 + chunk, H);
+      const int m0 = min(g.sub * chunk, H), m1 = min(m0 + chunk, H);
       double run = 0.0;
-      for (int m = m0; m < m1; ++m) run += xl[2 * m + 1];
+      if (valid)
+        for (int m = m0; m < m1; ++m) run += xl[2 * m + 1];
       double incl = run;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        double v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
+      for (int o = 1; o < g.L; o <<= 1) {
+        const double v = __shfl_up_sync(0xffffffffu, incl, o, g.L);
+        if (g.sub >= o) incl += v;
       }
+      if (!valid) continue;
       double pre = incl - run;  // exclusive prefix of this lane's chunk
       if (ds.has_post) {
         for (int m = m0; m < m1; ++m) {
@@ -1133,23 +1169,6 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
 // line, log2 L shuffle steps instead of 32 lanes and 5), and the fold is one FMA per point:
 // u_m = (x_m + x_{N-m})/2 - sin(pi m/N) (x_m - x_{N-m}) = x_{N-m} + (1/2 - sin(pi m/N)) (x_m - x_{N-m}).
 
-// Radix plan of the length-N FFT: every factor 3 first (the first stage has no twiddles, and a
-// twiddled radix-3 stage costs the most FP64 instructions per point), then 4s, then one 2.
-struct RadixPlan {
-  int n3, n4, n2;  // stages of radix 3, then 4, then 2
-  __device__ __forceinline__ int stages() const { return n3 + n4 + n2; }
-  __device__ __forceinline__ int at(int s) const { return s < n3 ? 3 : (s < n3 + n4 ? 4 : 2); }
-};
-__device__ __forceinline__ RadixPlan radix_plan(int N, int& rest) {
-  RadixPlan p{0, 0, 0};
-  int m = N;
-  while (m % 3 == 0) { ++p.n3; m /= 3; }
-  while (m % 4 == 0) { ++p.n4; m /= 4; }
-  if (m % 2 == 0) { ++p.n2; m /= 2; }
-  rest = m;  // 1 for every length with a twiddle table (n - 1 = 2^a 3^b)
-  return p;
-}
-
 struct WarpPairs {
   int lane, w, nw, npw;  // lane, warp, warps of the CTA, pairs this warp owns
 };
@@ -1162,34 +1181,12 @@ __device__ __forceinline__ WarpPairs warp_pairs(const Ctx& c, int nall) {
   return g;
 }
 
-template <int R>
-__device__ __forceinline__ void butterfly_plain(double2* v, double2* o) {
-  if (R == 2) {
-    o[0] = cadd(v[0], v[1]);
-    o[1] = csub(v[0], v[1]);
-  } else if (R == 4) {
-    double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    double2 e = cadd(v[1], v[3]), f = csub(v[1], v[3]);
-    o[0] = cadd(a, e);
-    o[2] = csub(a, e);
-    o[1] = make_double2(b.x + f.y, b.y - f.x);  // b - i f
-    o[3] = make_double2(b.x - f.y, b.y + f.x);  // b + i f
-  } else {  // R == 3, W3 = -1/2 - i sqrt(3)/2
-    const double h = 0.86602540378443864676;
-    double2 t1 = cadd(v[1], v[2]);
-    double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
-    double2 t3 = csub(v[1], v[2]);
-    o[0] = cadd(v[0], t1);
-    o[1] = make_double2(fma(h, t3.y, t2.x), fma(-h, t3.x, t2.y));  // t2 - i h t3
-    o[2] = make_double2(fma(-h, t3.y, t2.x), fma(h, t3.x, t2.y));  // t2 + i h t3
-  }
-}
-
 // First stage (Ns = 1, no twiddles) with the fold on its way in, over the warp's pairs.
 template <int R>
 __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2* dst, const double2* tw, int N,
                                       int npairs, int slot0, const DctScale& ds) {
   const int B = N / R;
+  const double* cmt = reinterpret_cast<const double*>(tw + 2 * N);
   for (int it = g.lane; it < g.npw * B; it += 32) {
     const int q = it / B, j = it - q * B;
     const int P = g.w + q * g.nw;
@@ -1201,7 +1198,7 @@ __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2*
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int m = j + r * B;
-      const double cm = 0.5 + __ldg(&tw[m].y);  // 1/2 - sin(pi m / N)
+      const double cm = __ldg(cmt + m);  // 1/2 - sin(pi m / N), after the 2N twiddles
       const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
       double ua = fma(cm, a0 - a1, a1);
       double ub = 0.0;
@@ -1278,6 +1275,11 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
   const WarpPairs g = warp_pairs(c, nall);
   if (g.npw == 0) return;
+  // A radix-4 stage and two radix-2 stages issue the same FP64 instructions per point, but the
+  // warp's butterfly count per stage (npw N / R) leaves different numbers of lanes idle in its last
+  // iteration: take radix 2 where that needs fewer FP64 warp instructions (6 per radix-2 butterfly
+  // and level, 24 per radix-4 butterfly and two levels).
+  const RadixPlan wplan = 6 * ((g.npw * N + 63) >> 6) < 12 * ((g.npw * N + 127) >> 7) ? radix_plan(N, rest, true) : plan;
   const int nl = 2 * g.npw;  // lines of the warp's pairs (the last one of an odd tile may not exist)
   const int L = lanes_per_line(nl), per = 32 / L, grp = g.lane / L, sub = g.lane & (L - 1);
 
@@ -1303,14 +1305,14 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   }
   // FFT of length N over the warp's pairs, ping-pong between the two buffers
   double2* bufs[2] = {c.f0, c.f1};
-  const int R0 = plan.at(0);
+  const int R0 = wplan.at(0);
   if (R0 == 3) wfold<3>(c, g, bufs[1], tw, N, npairs, op.a, ds);
   else if (R0 == 4) wfold<4>(c, g, bufs[1], tw, N, npairs, op.a, ds);
   else wfold<2>(c, g, bufs[1], tw, N, npairs, op.a, ds);
   int cur = 1, Ns = R0;
-  for (int s = 1; s < plan.stages(); ++s) {
+  for (int s = 1; s < wplan.stages(); ++s) {
     __syncwarp();
-    const int R = plan.at(s);
+    const int R = wplan.at(s);
     if (R == 4) wstage<4>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);
     else if (R == 2) wstage<2>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);
     else wstage<3>(c, g, bufs[cur], bufs[cur ^ 1], tw, N, Ns, 2);

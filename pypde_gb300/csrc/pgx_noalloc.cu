@@ -29,12 +29,14 @@ bool pgx_fft_length_ok(int n);
 
 namespace {
 
-constexpr int kTwiddles = 2 * PGX_LMAX;  // complex entries per table, >= 2(n-1) for every allowed n
+// complex entries per table: 2(n-1) twiddles and (n-1) / 2 for the n-1 fold coefficients, for every allowed n
+constexpr int kTwiddles = 3 * PGX_LMAX;
 
 static __device__ __align__(256) double g_noalloc_scratch[PGX_NOALLOC_SCRATCH_DOUBLES];
 static __device__ __align__(256) double2 g_noalloc_twiddles[2 * kTwiddles];
 
-// exp(-2 pi i k / L) for both axes' lengths; exact on the axes of the unit circle.
+// exp(-2 pi i k / L) for both axes' lengths, exact on the axes of the unit circle, each table
+// followed by the fold coefficients 0.5 + Im(tw[k]) = 1/2 - sin(2 pi k / L) (k < L / 2).
 __global__ void noalloc_fill_twiddles(int L0, int L1) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L0 + L1; i += gridDim.x * blockDim.x) {
     const int table = i < L0 ? 0 : 1;
@@ -48,6 +50,7 @@ __global__ void noalloc_fill_twiddles(int L0, int L1) {
       s = q == 1 ? 1.0 : (q == 3 ? -1.0 : 0.0);
     }
     g_noalloc_twiddles[table * kTwiddles + k] = make_double2(c, -s);
+    if (k < L / 2) reinterpret_cast<double*>(g_noalloc_twiddles + table * kTwiddles + L)[k] = 0.5 + (-s);
   }
 }
 
