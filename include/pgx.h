@@ -98,9 +98,14 @@ enum pgx_opcode {
 enum pgx_dct_mode { PGX_DCT_RAW = 0, PGX_DCT_FWD = 1, PGX_DCT_BWD = 2, PGX_DCT_FWD_T = 3, PGX_DCT_BWD_T = 4 };
 /* op.k of DCT: the mode in the low bits; PGX_DCT_CTA runs an even-length transform with its
  * phases spread over the whole CTA (block barriers between FFT stages) instead of one warp per
- * line pair. */
+ * line pair.  PGX_DCT_SLOT runs the FFT of a one-slot op (b <= 1) in the slot's own lines and the
+ * spare slot instead of separate buffers; it needs an even tile (tb) and a length n whose n - 1 is
+ * even with an FFT stage count that can be made odd (n - 1 = 2^p 3^b with p >= 2, or p = 1 and b
+ * even), and refuses other lengths (NaN).  When every DCT op of a program has it, the program
+ * takes no FFT buffers of shared memory. */
 #define PGX_DCT_MODE_MASK 7
 #define PGX_DCT_CTA 8
+#define PGX_DCT_SLOT 16
 
 /* Chain ops (DIFF, TDMA2, FDMA) act on the b consecutive slots a..a+b-1 at
  * once (b <= 1: slot a only); BANDED uses b as its first diagonal offset.

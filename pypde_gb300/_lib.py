@@ -19,6 +19,7 @@ OP = dict(LOAD=1, LOAD_ADD=2, LOAD_MUL=3, STORE=4, STORE_ADD=5, SCALE=6, AXPY=7,
 DCT_RAW, DCT_FWD, DCT_BWD, DCT_FWD_T, DCT_BWD_T = 0, 1, 2, 3, 4
 CHAIN_WARP = 1  # op.k flag of the chain ops: one warp per chain (PGX_CHAIN_WARP)
 DENSE_MMA = 2   # op.k flag of DENSE: contraction on the FP64 tensor cores (PGX_DENSE_MMA)
+DCT_SLOT = 16   # op.k flag of DCT: the FFT in the slot's own lines and the spare (PGX_DCT_SLOT)
 MAX_THREADS, MAX_THREADS_FFT = 1024, 768  # largest CTA; with DCT ops (PGX_MAX_THREADS[_FFT])
 
 

@@ -90,6 +90,8 @@ static int check_program_shape(const pgx_program* P) {
     const bool chain = op.code == PGX_OP_DIFF || op.code == PGX_OP_DIFF_T || op.code == PGX_OP_TDMA2 ||
                        op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T;
     if ((chain || op.code == PGX_OP_DCT) && op.a + (op.b > 1 ? op.b : 1) > P->nslots) return PGX_E_ARG;
+    // a DCT in the slot's own lines: one slot, line pairs filling the tile
+    if (op.code == PGX_OP_DCT && (op.k & PGX_DCT_SLOT) && (op.b > 1 || (P->tb & 1))) return PGX_E_ARG;
     if (chain && (op.code == PGX_OP_FDMA || op.code == PGX_OP_FDMA_T) && op.mat + (op.b > 1 ? op.b : 1) > PGX_MAX_MAT)
       return PGX_E_ARG;
     if (op.arr >= PGX_MAX_ARR || op.mat >= PGX_MAX_MAT || op.len >= PGX_MAX_LEN || op.par >= PGX_MAX_PAR) return PGX_E_ARG;

@@ -56,6 +56,17 @@ __host__ __device__ inline bool pgx_fft_in_spare(const pgx_program& P) {
   return 2LL * pgx_fft_stride(P.fft_n) * ((P.tb + 1) / 2) <= (long long)P.tb * P.lcap;
 }
 
+// Every DCT op of the program runs in its slot's own lines and the spare (PGX_DCT_SLOT): no FFT buffers.
+__host__ __device__ inline bool pgx_fft_in_slot(const pgx_program& P) {
+  bool any = false;
+  for (int o = 0; o < P.nops; ++o)
+    if (P.ops[o].code == PGX_OP_DCT) {
+      if (!(P.ops[o].k & PGX_DCT_SLOT)) return false;
+      any = true;
+    }
+  return any && !(P.tb & 1);
+}
+
 namespace pgx {
 
 // 2k for k < PGX_LMAX: multipliers of the derivative recurrence, read through
@@ -967,6 +978,17 @@ __device__ __forceinline__ RadixPlan radix_plan(int N, int& rest, bool radix2 = 
   return p;
 }
 
+// The plan with an odd number of stages, for a transform that ping-pongs between the slot and the
+// spare (the first stage reads the slot and writes the spare, so the last one writes the spare
+// too): one radix-4 stage split into two radix-2 stages (the same FP64 instructions per point), or
+// two radix-2 stages merged; no stages when neither exists (N = 2 * 3^b with b odd).
+__device__ __forceinline__ RadixPlan odd_stages(RadixPlan p) {
+  if (p.stages() & 1) return p;
+  if (p.n4 > 0) return RadixPlan{p.n3, p.n4 - 1, p.n2 + 2};
+  if (p.n2 >= 2) return RadixPlan{p.n3, p.n4 + 1, p.n2 - 2};
+  return RadixPlan{0, 0, 0};
+}
+
 // Untwiddled radix-R butterfly (the first stage of an FFT).
 template <int R>
 __device__ __forceinline__ void butterfly_plain(double2* v, double2* o) {
@@ -1056,8 +1078,10 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
   const int npairs = (c.tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
   int rest = 1;
-  const RadixPlan plan = radix_plan(N, rest);
-  if (N > c.fft_stride || rest != 1 || plan.stages() < 1) {  // no buffer or plan for this length: refuse loudly
+  const bool in_slot = (op.k & PGX_DCT_SLOT) != 0;
+  const RadixPlan plan = in_slot ? odd_stages(radix_plan(N, rest)) : radix_plan(N, rest);
+  if (N > c.fft_stride || rest != 1 || plan.stages() < 1 || (in_slot && (ns != 1 || (c.tb & 1)))) {
+    // no buffer or plan for this length: refuse loudly
     for (int sl = 0; sl < ns; ++sl)
       for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
     return;
@@ -1124,6 +1148,7 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
       if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
     }
   }
+  if (in_slot) zero_tail(c, slot_ptr(c, op.a), n);  // the FFT stages wrote past the lines' ends
   __syncthreads();
   // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1, L lanes a line
   {
@@ -1267,8 +1292,11 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int npairs = (c.tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
   int rest = 1;
+  const bool in_slot = (op.k & PGX_DCT_SLOT) != 0;
   const RadixPlan plan = radix_plan(N, rest);
-  if (N > c.fft_stride || rest != 1 || plan.stages() < 1) {  // no buffer or plan for this length: refuse loudly
+  if (N > c.fft_stride || rest != 1 || plan.stages() < 1 ||
+      (in_slot && (ns != 1 || (c.tb & 1) || odd_stages(plan).stages() < 1))) {
+    // no buffer or plan for this length: refuse loudly
     for (int sl = 0; sl < ns; ++sl)
       for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
     return;
@@ -1279,7 +1307,8 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   // warp's butterfly count per stage (npw N / R) leaves different numbers of lanes idle in its last
   // iteration: take radix 2 where that needs fewer FP64 warp instructions (6 per radix-2 butterfly
   // and level, 24 per radix-4 butterfly and two levels).
-  const RadixPlan wplan = 6 * ((g.npw * N + 63) >> 6) < 12 * ((g.npw * N + 127) >> 7) ? radix_plan(N, rest, true) : plan;
+  RadixPlan wplan = 6 * ((g.npw * N + 63) >> 6) < 12 * ((g.npw * N + 127) >> 7) ? radix_plan(N, rest, true) : plan;
+  if (in_slot) wplan = odd_stages(wplan);  // the last stage writes the spare, not the slot
   const int nl = 2 * g.npw;  // lines of the warp's pairs (the last one of an odd tile may not exist)
   const int L = lanes_per_line(nl), per = 32 / L, grp = g.lane / L, sub = g.lane & (L - 1);
 
@@ -1347,6 +1376,15 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
     }
   }
+  if (in_slot) {  // the FFT stages wrote past the ends of the warp's lines: zero [n, lcap) again
+    const int w = c.lcap - n;
+    double* x = slot_ptr(c, op.a);
+    for (int it = g.lane; it < g.npw * 2 * w; it += 32) {
+      const int q = it / (2 * w), r = it - q * 2 * w;
+      const int t = 2 * (g.w + q * g.nw) + (r >= w ? 1 : 0);  // one slot: pair P = line pair P
+      x[t * c.lcap + n + (r >= w ? r - w : r)] = 0.0;
+    }
+  }
   __syncwarp();
   // odd outputs: inclusive prefix sums over k = 1, 3, ..., N-1, L lanes a line
   {
@@ -1399,6 +1437,11 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     return;
   }
   const int ns = nslot_of(op);  // paired-line path: one slot after the other
+  if (op.k & PGX_DCT_SLOT) {  // needs 2(n - 1) complex values a pair: no room in the slot, refuse loudly
+    for (int sl = 0; sl < ns; ++sl)
+      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+    return;
+  }
   for (int sl = 0; sl < ns; ++sl) {
     dct_paired_slot(c, op.a + sl, op, I);
     __syncthreads();
@@ -1472,10 +1515,13 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   size_t off = (size_t)nbuf * c.tb * c.lcap;
   c.fft_stride = pgx_fft_stride(P.fft_n);
   const int fs = pgx_fft_slots(P);
-  const bool fft_in_spare = FFT && pgx_fft_in_spare(P);
-  c.f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
-  c.f1 = fft_in_spare ? nullptr : c.f0 + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride;
-  c.ybuf = reinterpret_cast<double*>((fft_in_spare ? c.f0 : c.f1) + (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride);
+  const bool in_slot = FFT && pgx_fft_in_slot(P);
+  const bool fft_in_spare = FFT && !in_slot && pgx_fft_in_spare(P);
+  const size_t fbuf = in_slot ? 0 : (size_t)fs * ((c.tb + 1) >> 1) * c.fft_stride;
+  double2* const f0 = reinterpret_cast<double2*>(c.sm + off + (off & 1));
+  double2* const f1 = fft_in_spare ? nullptr : f0 + fbuf;
+  c.ybuf = reinterpret_cast<double*>((fft_in_spare || in_slot ? f0 : f1) + fbuf);
+  const int fft_stride = c.fft_stride;
   for (int s = 0; s < nbuf; ++s) c.phys[s] = s;
   for (int s = 0; s < PGX_MAX_SLOTS; ++s) c.slen[s] = 0;
   c.spare = P.nslots;
@@ -1503,7 +1549,15 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
       case PGX_OP_DIFF: op_diff(c, op); break;
       case PGX_OP_DCT:
         if (FFT) {  // programs with DCT ops run the FFT kernels only
-          if (fft_in_spare) c.f1 = reinterpret_cast<double2*>(spare_ptr(c));  // even tb: 16-byte aligned
+          if (op.k & PGX_DCT_SLOT) {  // ping-pong between the slot's own line pairs and the spare
+            c.f0 = reinterpret_cast<double2*>(slot_ptr(c, op.a));  // even tb: 16-byte aligned
+            c.f1 = reinterpret_cast<double2*>(spare_ptr(c));
+            c.fft_stride = c.lcap;  // a pair's two lines, in complex elements
+          } else {
+            c.f0 = in_slot ? nullptr : f0;
+            c.f1 = fft_in_spare ? reinterpret_cast<double2*>(spare_ptr(c)) : f1;
+            c.fft_stride = in_slot ? 0 : fft_stride;
+          }
           op_dct(c, op, I);
         }
         break;
@@ -1651,7 +1705,8 @@ extern "C" int64_t pgx_program_smem(const pgx_program* P) {
   int64_t doubles = nbuf * P->tb * P->lcap;
   doubles += doubles & 1;
   const int64_t fs = pgx_fft_slots(*P);
-  const int64_t nbufs = pgx_fft_in_spare(*P) ? 1 : 2;  // the second FFT buffer may live in the spare slot
+  // no FFT buffers (transforms in the slots), or the second one in the spare slot
+  const int64_t nbufs = pgx_fft_in_slot(*P) ? 0 : (pgx_fft_in_spare(*P) ? 1 : 2);
   if (P->fft_n > 1) doubles += nbufs * 2 * fs * (int64_t)((P->tb + 1) / 2) * pgx_fft_stride(P->fft_n) + fs * P->tb + 1;
   return doubles * 8;
 }

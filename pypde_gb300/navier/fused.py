@@ -835,14 +835,34 @@ CHAIN_OPS = ("FDMA", "POISSON", "TDMA2", "FDMA_T", "POISSON_T")
 _CHAIN_CODES = tuple(_lib.OP[k] for k in CHAIN_OPS)
 
 
+def dct_in_slot_ok(fft_n):
+    """Whether a DCT of length ``fft_n`` can run in its slot's own lines and the spare slot
+    (PGX_DCT_SLOT): n - 1 even, with an FFT stage count that can be made odd (n - 1 = 2^p 3^b
+    with p >= 2, or p = 1 and b even)."""
+    N = fft_n - 1
+    if N < 2 or N % 2:
+        return False
+    p = b = 0
+    while N % 2 == 0:
+        N //= 2
+        p += 1
+    while N % 3 == 0:
+        N //= 3
+        b += 1
+    return N == 1 and (p >= 2 or b % 2 == 0)
+
+
 def fft_bytes_per_line(fft_n, one_slot=False):
     """Shared memory of the DCT-I work buffers per line: two buffers of n-1 (folded algorithm,
     even n-1) or 2(n-1) (paired lines) complex values per pair of lines, plus one scalar.  With
-    ``one_slot`` (every DCT op transforms one slot) and the folded algorithm the second buffer is
+    ``one_slot`` (every DCT op transforms one slot) and the folded algorithm the transforms run in
+    the slots' own lines and the spare slot (lengths ``dct_in_slot_ok``) or the second buffer is
     the spare slot (for an even number of lines per tile)."""
     if fft_n <= 1:
         return 0
     even = (fft_n - 1) % 2 == 0
+    if one_slot and dct_in_slot_ok(fft_n):
+        return 8
     stride = fft_n - 1 if even else 2 * (fft_n - 1)
     return (8 if (one_slot and even) else 16) * stride + 8
 SMEM_PER_SM = 227 * 1024
@@ -986,6 +1006,30 @@ def launch_ops(prog, sd=False, dm=False):
     return ops
 
 
+def launch_program(prog, key, tb, nt, wc=False, sd=False, dm=False):
+    """The PgxProgram of one launch of ``prog`` for the size class ``key`` = (lcap, fft_n) with
+    ``tb`` lines and ``nt`` threads a CTA (``wc``, ``sd``, ``dm`` as in ``FusedBatch._group_launch``).
+    One-slot transforms of the pass's (dealiased) length on even tiles run in the slots' own lines
+    (PGX_DCT_SLOT): no FFT buffers of shared memory."""
+    lcap, fft_n = key
+    ops = launch_ops(prog, sd, dm)
+    if dm:
+        fft_n = 0
+    P = _lib.PgxProgram()
+    P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
+    P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), fft_n, nt
+    assert len(ops) <= _lib.MAX_OPS, (prog.name, len(ops))
+    dct = [o for o in ops if o.code == _lib.OP["DCT"]]
+    in_slot = bool(dct) and tb % 2 == 0 and all(o.b <= 1 for o in dct) and dct_in_slot_ok(fft_n)
+    for i, o in enumerate(ops):
+        P.ops[i] = o
+        if wc and o.code in _CHAIN_CODES:
+            P.ops[i].k = o.k | _lib.CHAIN_WARP
+        if in_slot and o.code == _lib.OP["DCT"]:
+            P.ops[i].k = o.k | _lib.DCT_SLOT
+    return P
+
+
 class FusedBatch:
     """Fused Euler step for a batch of NavierStokes instances (any sizes / Ra)."""
 
@@ -1069,18 +1113,7 @@ class FusedBatch:
         """One launch of ``prog`` over ``members``; ``wc``: chain ops in warp-per-chain mode;
         ``sd``: multi-slot DCT ops as one op per slot; ``dm``: DCT ops as dense matrices and every
         DENSE op on the FP64 tensor cores (no FFT buffers)."""
-        lcap, fft_n = key
-        ops = launch_ops(prog, sd, dm)
-        if dm:
-            fft_n = 0
-        P = _lib.PgxProgram()
-        P.axis, P.lines_len, P.tb, P.lcap = prog.axis, L_LINES, tb, lcap
-        P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), fft_n, nt
-        assert len(ops) <= _lib.MAX_OPS, (prog.name, len(ops))
-        for i, o in enumerate(ops):
-            P.ops[i] = o
-            if wc and o.code in _CHAIN_CODES:
-                P.ops[i].k = o.k | _lib.CHAIN_WARP
+        P = launch_program(prog, key, tb, nt, wc, sd, dm)
         nv = len(prog.variants)
         # the batched launch cannot read its descriptors on the host: check every member's host copy
         host = getattr(d_insts, "pgx_host", None)

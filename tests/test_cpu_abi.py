@@ -116,6 +116,53 @@ def test_program_checks_reject_malformed_dct_ops():
     assert _lib.MAX_THREADS == 1024 and _lib.MAX_THREADS_FFT == 768
 
 
+def test_in_slot_dct_flag():
+    """PGX_DCT_SLOT (the FFT of a one-slot DCT op in the slot's own lines and the spare slot):
+    pgx_program_smem drops the FFT buffers when every DCT op has it, pgx_run refuses it on a
+    multi-slot op or an odd tile, and the host's length rule (dct_in_slot_ok) holds exactly for the
+    even lengths whose radix plan (3s, then 4s, then one 2) has, or can be given by splitting a
+    radix-4 stage or merging two radix-2 stages, an odd number of stages."""
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import dct_in_slot_ok
+    L = _lib.lib()
+
+    def prog(k, b=1, tb=4):
+        P = _lib.PgxProgram()
+        P.axis, P.lines_len, P.tb, P.lcap, P.nslots, P.fft_n, P.nthreads = 0, 1, tb, 195, 2, 193, 128
+        ops = [_lib.op("LOAD", a=0, arr=0, len=0), _lib.op("DCT", a=0, b=b, mat=0, k=k), _lib.op("STORE", a=0, arr=1)]
+        P.nops = len(ops)
+        for i, o in enumerate(ops):
+            P.ops[i] = o
+        return P
+
+    plain = L.pgx_program_smem(ctypes.byref(prog(_lib.DCT_FWD)))
+    slot = L.pgx_program_smem(ctypes.byref(prog(_lib.DCT_FWD | _lib.DCT_SLOT)))
+    # 3 slot buffers of 4 x 195, the y_1 scalars (4 + 1); without the flag one FFT buffer of 2 pairs
+    # x 192 complex values (the second is the spare slot)
+    assert slot == 8 * (3 * 4 * 195 + 5) and plain == slot + 8 * 2 * 2 * 192
+    inst = _lib.PgxInstance()
+    for P in (prog(_lib.DCT_FWD | _lib.DCT_SLOT, b=2), prog(_lib.DCT_FWD | _lib.DCT_SLOT, tb=3)):
+        assert L.pgx_run(ctypes.byref(P), ctypes.byref(inst), None) == 1   # PGX_E_ARG
+
+    def odd_plan_exists(n):
+        N = n - 1
+        if N < 2 or N % 2:
+            return False
+        m, n3, n4, n2 = N, 0, 0, 0
+        while m % 3 == 0:
+            m, n3 = m // 3, n3 + 1
+        while m % 4 == 0:
+            m, n4 = m // 4, n4 + 1
+        if m % 2 == 0:
+            m, n2 = m // 2, n2 + 1
+        if m != 1:
+            return False
+        return (n3 + n4 + n2) % 2 == 1 or n4 > 0 or n2 >= 2
+
+    assert all(dct_in_slot_ok(n) == odd_plan_exists(n) for n in range(2, _lib.LMAX))
+    assert [n for n in (7, 9, 17, 33, 49, 55, 97, 193) if dct_in_slot_ok(n)] == [9, 17, 33, 49, 97, 193]
+
+
 def test_instance_checks_on_host_descriptors():
     """pgx_check_instance (no device needed) accepts a consistent descriptor and refuses one whose
     array is longer than the slot capacity, whose length exceeds it, or whose table is missing."""
@@ -151,7 +198,7 @@ def test_tile_candidates_fit_the_launch_limits(shape):
     check pgx_run_batched makes) and the thread limit of the kernel build it runs on."""
     import ctypes
     from pypde_gb300 import _lib
-    from pypde_gb300.navier.fused import (L_ND, _candidates, _pick, build_programs, instance_params, launch_ops,
+    from pypde_gb300.navier.fused import (L_ND, _candidates, _pick, build_programs, instance_params, launch_program,
                                           program_maxlen)
     from pypde_gb300.navier.fused_adjoint import build_adjoint_programs
     N, M = shape
@@ -167,13 +214,8 @@ def test_tile_candidates_fit_the_launch_limits(shape):
         tiles = _candidates(prog, lines * len(prog.variants), lcap, fft_n, lines)
         tiles.append(_pick(prog, lines * len(prog.variants), lcap, fft_n, lines))
         for tb, nt, wc, sd, dm in tiles:
-            ops = launch_ops(prog, sd, dm)
-            P = _lib.PgxProgram()
-            P.axis, P.lines_len, P.tb, P.lcap = prog.axis, 0, tb, lcap
-            P.nslots, P.nops, P.fft_n, P.nthreads = prog.nslots, len(ops), 0 if dm else fft_n, nt
-            for i, o in enumerate(ops):
-                P.ops[i] = o
+            P = launch_program(prog, (lcap, fft_n), tb, nt, wc, sd, dm)
             smem = _lib.smem_bytes(P)
             assert smem + desc + 1024 <= limit, (prog.name, shape, tb, nt, sd, dm, smem)
-            has_dct = any(o.code == _lib.OP["DCT"] for o in ops)
+            has_dct = any(P.ops[i].code == _lib.OP["DCT"] for i in range(P.nops))
             assert nt % 32 == 0 and nt <= (_lib.MAX_THREADS_FFT if has_dct else _lib.MAX_THREADS), (prog.name, nt)

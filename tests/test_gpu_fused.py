@@ -160,8 +160,10 @@ def test_warp_parallel_chains_match_sequential(NS):
 
 def test_joint_and_serial_dct_ops_agree(NS):
     """Multi-slot DCT ops (all slots' lines through each transform phase together) give the
-    result of one DCT op per slot exactly; 97-point lines take the folded even path, 28-point
-    lines the paired-line path."""
+    result of one DCT op per slot to rounding (the one-slot ops of even tiles run in the slots' own
+    lines with an odd number of FFT stages, the multi-slot ops in FFT buffers); 97-point lines take
+    the folded even path, 28-point lines the paired-line path."""
+    from pypde_gb300 import _lib
     from pypde_gb300.navier.fused import FusedBatch, _fft_slots
     specs = [((65, 33), 1e5, 1), ((19, 33), 1e4, 2)]
     outs = []
@@ -177,12 +179,51 @@ def test_joint_and_serial_dct_ops_agree(NS):
         fb._build_launches(tiles)
         joint = [L for g in fb.launches for L in g if _fft_slots(L["prog"]) > 1]
         assert joint and all(L["sd"] == sd for L in joint)
+        in_slot = [L for L in joint if any(L["P"].ops[i].code == _lib.OP["DCT"] and L["P"].ops[i].k & _lib.DCT_SLOT
+                                           for i in range(L["P"].nops))]
+        assert bool(in_slot) == sd
         for _ in range(3):
             fb.step_eager()
         outs.append([ns.state() for ns in solvers])
     for a, b in zip(*outs):
         for k in a:
-            assert np.array_equal(a[k], b[k]), k
+            assert rel_err(b[k], a[k]) < 1e-12, k
+
+
+@pytest.mark.parametrize("dealias", [True, False])
+def test_in_slot_dct_vs_oracle(NS, dealias):
+    """DCT ops run in the slot's own lines and the spare slot (PGX_DCT_SLOT: one-slot ops, even
+    tiles, the FFT stage count made odd -- 96-, 128- and 192-point FFTs change plan, 32-, 48- and
+    64-point ones keep theirs) in the CTA-wide form (4 lines, 256 threads) and the warp-local form
+    (16 lines, 64 threads): each instance follows its oracle for three steps."""
+    from pypde_gb300 import _lib
+    from pypde_gb300.navier.fused import FusedBatch
+    specs = [((33, 65), 1e4, 100), ((129, 33), 1e5, 101), ((65, 129), 3e6, 102)]
+    for tb, nt in ((4, 256), (16, 64)):
+        solvers = []
+        for shape, ra, seed in specs:
+            ns = NS(case="linear", shape=shape, ra=ra, pr=1.0, dt=0.005, dealias=dealias, integrator="eu",
+                    tsave=None)
+            ns.set_temperature_noise(seed, 1e-3)
+            solvers.append(ns)
+        fb = FusedBatch(solvers)
+        assert fb.fft
+        names = [p.name for p in fb.progs]
+        tiles = {}
+        for tag, tile in fb.tiles().items():
+            prog = fb.progs[names.index(tag.split("#")[0])]
+            tiles[tag] = (tb, nt, False, True, False) if prog.has_dct else tile
+        fb._build_launches(tiles)
+        flagged = [L for g in fb.launches for L in g
+                   if any(L["P"].ops[i].code == _lib.OP["DCT"] and L["P"].ops[i].k & _lib.DCT_SLOT
+                          for i in range(L["P"].nops))]
+        dct_launches = [L for g in fb.launches for L in g if L["prog"].has_dct]
+        assert flagged and len(flagged) == len(dct_launches)
+        for _ in range(3):
+            fb.step_eager()
+        for ns, (shape, ra, seed) in zip(solvers, specs):
+            ref = oracle_run("linear", shape, dict(ra=ra, dt=0.005, dealias=dealias), seed, 1e-3, 3)
+            compare(ns, ref, 1e-8)
 
 
 def test_tensor_core_contractions_match(NS):
