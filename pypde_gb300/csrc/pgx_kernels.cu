@@ -97,6 +97,10 @@ struct Ctx {
 __device__ __forceinline__ double* slot_ptr(const Ctx& c, int s) {
   return c.sm + (size_t)c.phys[s] * c.tb * c.lcap;
 }
+// Slot s0 + sl of a multi-slot op whose slot s0 is x0: sl == 0 (every one-slot op) reads no slot map.
+__device__ __forceinline__ double* op_slot(const Ctx& c, double* x0, int s0, int sl) {
+  return sl == 0 ? x0 : slot_ptr(c, s0 + sl);
+}
 __device__ __forceinline__ double* spare_ptr(const Ctx& c) {
   return c.sm + (size_t)c.spare * c.tb * c.lcap;
 }
@@ -129,17 +133,27 @@ __device__ __forceinline__ View view_of(const pgx_array& a, int axis) {
 
 // Zero [from, lcap) of every line of buffer `b`.
 __device__ void zero_tail(const Ctx& c, double* b, int from) {
-  int w = c.lcap - from;
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  int w = c_lcap - from;
   if (w <= 0) return;
-  for (int idx = c.tid; idx < c.tb * w; idx += c.nthreads) {
+  for (int idx = c_tid; idx < c_tb * w; idx += c_nthreads) {
     int t = idx / w, i = from + idx % w;
-    b[t * c.lcap + i] = 0.0;
+    b[t * c_lcap + i] = 0.0;
   }
 }
 
 // ------------------------------------------------------------------ load/store
 // mode 0: slot = alpha*arr (length n, zero beyond the array), 1: +=, 2: *=
 __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, int mode) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_l0 = c.l0;
+  const int c_nlines = c.nlines;
   const View v = view_of(I.arr[op.arr], axis);
   const double alpha = op_alpha(op, I);
   int n;
@@ -150,16 +164,16 @@ __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axi
     n = c.slen[op.a];
   }
   double* s = slot_ptr(c, op.a);
-  const int tb = c.tb;
+  const int tb = c_tb;
   const bool contig = (v.se == 1);
-  for (int idx = c.tid; idx < tb * n; idx += c.nthreads) {
+  for (int idx = c_tid; idx < tb * n; idx += c_nthreads) {
     int t, i;
     if (contig) { t = idx / n; i = idx - t * n; }
     else { i = idx / tb; t = idx - i * tb; }
-    const int line = c.l0 + t;
+    const int line = c_l0 + t;
     double x = 0.0;
-    if (i < v.ne && line < v.nl && line < c.nlines) x = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
-    double* d = s + t * c.lcap + i;
+    if (i < v.ne && line < v.nl && line < c_nlines) x = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
+    double* d = s + t * c_lcap + i;
     if (mode == 0) *d = alpha == 1.0 ? x : alpha * x;
     else if (mode == 1) *d = fma(alpha, x, *d);
     else *d = (alpha == 1.0 ? x : alpha * x) * (*d);
@@ -171,19 +185,25 @@ __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axi
 }
 
 __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, bool add) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_l0 = c.l0;
+  const int c_nlines = c.nlines;
   const View v = view_of(I.arr[op.arr], axis);
   const double alpha = op_alpha(op, I);
   const double* s = slot_ptr(c, op.a);
   const int n = v.ne;
-  const int tb = c.tb;
+  const int tb = c_tb;
   const bool contig = (v.se == 1);
-  for (int idx = c.tid; idx < tb * n; idx += c.nthreads) {
+  for (int idx = c_tid; idx < tb * n; idx += c_nthreads) {
     int t, i;
     if (contig) { t = idx / n; i = idx - t * n; }
     else { i = idx / tb; t = idx - i * tb; }
-    const int line = c.l0 + t;
-    if (line >= v.nl || line >= c.nlines) continue;
-    double x = s[t * c.lcap + i];
+    const int line = c_l0 + t;
+    if (line >= v.nl || line >= c_nlines) continue;
+    double x = s[t * c_lcap + i];
     double* d = v.p + (int64_t)i * v.se + (int64_t)line * v.sl;
     if (add) *d = fma(alpha, x, *d);
     else *d = alpha == 1.0 ? x : alpha * x;
@@ -192,6 +212,10 @@ __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, 
 
 // ------------------------------------------------------------- pointwise ops
 __device__ void op_pointwise(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const double alpha = op_alpha(op, I);
   double* a = slot_ptr(c, op.a);
   const double* b = op.b >= 0 ? slot_ptr(c, op.b) : nullptr;
@@ -202,9 +226,9 @@ __device__ void op_pointwise(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     else if (nb > n) n = nb;
     c.slen[op.a] = n;
   }
-  for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
+  for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) {
     int t = idx / n, i = idx - t * n;
-    int o = t * c.lcap + i;
+    int o = t * c_lcap + i;
     switch (op.code) {
       case PGX_OP_SCALE: a[o] *= alpha; break;
       case PGX_OP_AXPY: a[o] = fma(alpha, b[o], a[o]); break;
@@ -228,15 +252,19 @@ __device__ void op_setlen(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 // ------------------------------------------------------------------ stencils
 // u_i = v_i [i < M] + s_{i-2} v_{i-2} [i >= 2],  s = S[i+2, i] sub-diagonal table.
 __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const double* sd = I.mat[op.mat];
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   const int M = c.slen[op.a], N = M + 2;
-  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
-    int t = idx / c.lcap, i = idx - t * c.lcap;
+  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
+    int t = idx / c_lcap, i = idx - t * c_lcap;
     double r = 0.0;
     if (i < N) {
-      const double* xl = x + t * c.lcap;
+      const double* xl = x + t * c_lcap;
       r = i < M ? xl[i] : 0.0;
       if (i >= 2) r = fma(__ldg(sd + i - 2), xl[i - 2], r);
     }
@@ -248,15 +276,19 @@ __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 
 // (S^T u)_i = u_i + s_i u_{i+2},  i < N-2.
 __device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const double* sd = I.mat[op.mat];
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   const int N = c.slen[op.a], M = N - 2;
-  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
-    int t = idx / c.lcap, i = idx - t * c.lcap;
+  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
+    int t = idx / c_lcap, i = idx - t * c_lcap;
     double r = 0.0;
     if (i < M) {
-      const double* xl = x + t * c.lcap;
+      const double* xl = x + t * c_lcap;
       r = fma(__ldg(sd + i), xl[i + 2], xl[i]);
     }
     y[idx] = r;
@@ -412,29 +444,33 @@ __device__ __forceinline__ void tdma_chain_warp(double* x, const double* tab, in
 //   g_i = (d_i - aa_i g_{i-2}) rden_i,  x_j = g_j - w_j x_{j+2}.
 // The last two w_i of a chain multiply x_{n}, x_{n+1} = 0 and are never used.
 __device__ void op_tdma2(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   int s, t, p;
   const int ns = nslot_of(op);
   if (op.k & PGX_CHAIN_WARP) {
-    const int lane = c.tid & 31, nw = c.nthreads >> 5;
-    for (int w = c.tid >> 5; w < 2 * c.tb * ns; w += nw) {
-      s = w / (2 * c.tb);
-      const int r = w - s * 2 * c.tb;
-      p = r / c.tb;
-      t = r - p * c.tb;
+    const int lane = c_tid & 31, nw = c_nthreads >> 5;
+    for (int w = c_tid >> 5; w < 2 * c_tb * ns; w += nw) {
+      s = w / (2 * c_tb);
+      const int r = w - s * 2 * c_tb;
+      p = r / c_tb;
+      t = r - p * c_tb;
       const int n = c.slen[op.a + s];
       if (p >= n) continue;
-      tdma_chain_warp(slot_ptr(c, op.a + s) + t * c.lcap, I.mat[op.mat], n, p, lane);
+      tdma_chain_warp(slot_ptr(c, op.a + s) + t * c_lcap, I.mat[op.mat], n, p, lane);
     }
     return;
   }
-  for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
+  for (int base = 0; base < 2 * c_tb * ns; base += c_nthreads) {
     Ctx cc = c;
-    cc.tid = c.tid + base;
+    cc.tid = c_tid + base;
     if (!chain_of(cc, ns, s, t, p)) continue;
     const int n = c.slen[op.a + s];
     if (p >= n) continue;
     const double* tab = I.mat[op.mat];
-    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    double* x = slot_ptr(c, op.a + s) + t * c_lcap;
     double g = 0.0;
     int i = p;
     for (; i < n; i += 2) {  // g_i = r_i x_i - (a r)_i g_{i-2}: one dependent FMA per step
@@ -482,14 +518,16 @@ __device__ __forceinline__ LineLanes line_lanes(const Ctx& c, int nl) {
 }
 
 __device__ void op_diff(Ctx& c, const pgx_op& op) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
   const int ns = nslot_of(op);
-  const LineLanes g = line_lanes(c, ns * c.tb);
+  const LineLanes g = line_lanes(c, ns * c_tb);
   for (int base = g.first; base < g.nl; base += g.stride) {  // the same trip count for the whole warp
     const int w = base + g.grp;
     const bool valid = w < g.nl;
-    const int s = valid ? w / c.tb : 0, t = valid ? w - s * c.tb : 0;
+    const int s = valid ? w / c_tb : 0, t = valid ? w - s * c_tb : 0;
     const int n = valid ? c.slen[op.a + s] : 0;
-    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    double* x = slot_ptr(c, op.a + s) + t * c_lcap;
     const int chunk = (n + g.L - 1) / g.L;
     const int a = min(g.sub * chunk, n), b = min(a + chunk, n);
     for (int rep = 0; rep < op.k; ++rep) {
@@ -524,14 +562,16 @@ __device__ void op_diff(Ctx& c, const pgx_op& op) {
 //   (D^T y)_i = 2i sum_{1 <= j < i, j = i+1 mod 2} y_j + y_0 [i odd] (1 if i = 1 else i).
 // Forward prefix sums per parity class, L lanes a line.
 __device__ void op_diff_t(Ctx& c, const pgx_op& op) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
   const int ns = nslot_of(op);
-  const LineLanes g = line_lanes(c, ns * c.tb);
+  const LineLanes g = line_lanes(c, ns * c_tb);
   for (int base = g.first; base < g.nl; base += g.stride) {
     const int w = base + g.grp;
     const bool valid = w < g.nl;
-    const int s = valid ? w / c.tb : 0, t = valid ? w - s * c.tb : 0;
+    const int s = valid ? w / c_tb : 0, t = valid ? w - s * c_tb : 0;
     const int n = valid ? c.slen[op.a + s] : 0;
-    double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+    double* x = slot_ptr(c, op.a + s) + t * c_lcap;
     const int chunk = (n + g.L - 1) / g.L;
     const int a = min(g.sub * chunk, n), b = min(a + chunk, n);
     for (int rep = 0; rep < op.k; ++rep) {
@@ -633,53 +673,63 @@ __device__ __forceinline__ void fdma_t_chain(double* x, const double* tab, int n
 }
 
 __device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool per_line, bool transpose = false) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_l0 = c.l0;
+  const int c_nlines = c.nlines;
   int s, t, p;
   const int ns = nslot_of(op);
   if (op.k & PGX_CHAIN_WARP) {
-    const int lane = c.tid & 31, nw = c.nthreads >> 5;
-    for (int w = c.tid >> 5; w < 2 * c.tb * ns; w += nw) {
-      s = w / (2 * c.tb);
-      const int r = w - s * 2 * c.tb;
-      p = r / c.tb;
-      t = r - p * c.tb;
+    const int lane = c_tid & 31, nw = c_nthreads >> 5;
+    for (int w = c_tid >> 5; w < 2 * c_tb * ns; w += nw) {
+      s = w / (2 * c_tb);
+      const int r = w - s * 2 * c_tb;
+      p = r / c_tb;
+      t = r - p * c_tb;
       const int n = c.slen[op.a + s];
-      const int line = c.l0 + t;
-      if (p >= n || line >= c.nlines) continue;
+      const int line = c_l0 + t;
+      if (p >= n || line >= c_nlines) continue;
       const double* tab = I.mat[op.mat + (per_line ? 0 : s)];
       if (per_line) tab += (size_t)line * 4 * n;
-      double* x = slot_ptr(c, op.a + s) + t * c.lcap;
+      double* x = slot_ptr(c, op.a + s) + t * c_lcap;
       if (transpose) fdma_t_chain_warp(x, tab, n, p, lane);
       else fdma_chain_warp(x, tab, n, p, lane);
     }
     return;
   }
-  for (int base = 0; base < 2 * c.tb * ns; base += c.nthreads) {
+  for (int base = 0; base < 2 * c_tb * ns; base += c_nthreads) {
     Ctx cc = c;
-    cc.tid = c.tid + base;
+    cc.tid = c_tid + base;
     if (!chain_of(cc, ns, s, t, p)) continue;
     const int n = c.slen[op.a + s];
-    const int line = c.l0 + t;
-    if (p >= n || line >= c.nlines) continue;
+    const int line = c_l0 + t;
+    if (p >= n || line >= c_nlines) continue;
     const double* tab = I.mat[op.mat + (per_line ? 0 : s)];
     if (per_line) tab += (size_t)line * 4 * n;
-    if (transpose) fdma_t_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
-    else fdma_chain(slot_ptr(c, op.a + s) + t * c.lcap, tab, n, p);
+    if (transpose) fdma_t_chain(slot_ptr(c, op.a + s) + t * c_lcap, tab, n, p);
+    else fdma_chain(slot_ptr(c, op.a + s) + t * c_lcap, tab, n, p);
   }
 }
 
 // --------------------------------------------------------- banded / dense
 __device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const double* A = I.mat[op.mat];
   const int rows = I.len[op.len];
   const int nd = op.k, off0 = op.b;
   const int cols = c.slen[op.a];
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
-  for (int idx = c.tid; idx < c.tb * c.lcap; idx += c.nthreads) {
-    int t = idx / c.lcap, r = idx - t * c.lcap;
+  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
+    int t = idx / c_lcap, r = idx - t * c_lcap;
     double acc = 0.0;
     if (r < rows) {
-      const double* xl = x + t * c.lcap;
+      const double* xl = x + t * c_lcap;
       for (int d = 0; d < nd; ++d) {
         int col = r + off0 + 2 * d;
         if (col >= 0 && col < cols) acc = fma(__ldg(A + d * rows + r), xl[col], acc);
@@ -702,21 +752,25 @@ __device__ __forceinline__ void dmma_8x8x4(double& d0, double& d1, double a, dou
 // y = A x per line on the tensor cores: Y (rows x tb) = A (rows x cols) X (cols x tb), one warp per
 // 8-row x 8-line output block, two accumulators over alternating column quads.
 __device__ void op_dense_mma(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const double* A = I.mat[op.mat];
   const int rows = I.len[op.len];
   const int cols = c.slen[op.a];
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   zero_tail(c, y, rows);
-  const int lane = c.tid & 31, warp = c.tid >> 5, nw = c.nthreads >> 5;
+  const int lane = c_tid & 31, warp = c_tid >> 5, nw = c_nthreads >> 5;
   const int g = lane >> 2, q = lane & 3;
-  const int nrb = (rows + 7) >> 3, nlb = (c.tb + 7) >> 3;
+  const int nrb = (rows + 7) >> 3, nlb = (c_tb + 7) >> 3;
   for (int blk = warp; blk < nrb * nlb; blk += nw) {  // warp-uniform loop
     const int lb = blk / nrb, rb = blk - lb * nrb;
     const int r = rb * 8 + g, t = lb * 8 + g;          // the A row / X line this lane loads
-    const bool rok = r < rows, tok = t < c.tb;
+    const bool rok = r < rows, tok = t < c_tb;
     const double* Ar = A + (size_t)(rok ? r : 0) * cols;
-    const double* xl = x + (tok ? t : 0) * c.lcap;
+    const double* xl = x + (tok ? t : 0) * c_lcap;
     double d0 = 0.0, d1 = 0.0, e0 = 0.0, e1 = 0.0;
     int k = 0;
     for (; k + 8 <= cols; k += 8) {
@@ -732,8 +786,8 @@ __device__ void op_dense_mma(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     }
     const int orow = rb * 8 + g, t0 = lb * 8 + 2 * q;
     if (orow < rows) {
-      if (t0 < c.tb) y[t0 * c.lcap + orow] = d0 + e0;
-      if (t0 + 1 < c.tb) y[(t0 + 1) * c.lcap + orow] = d1 + e1;
+      if (t0 < c_tb) y[t0 * c_lcap + orow] = d0 + e0;
+      if (t0 + 1 < c_tb) y[(t0 + 1) * c_lcap + orow] = d1 + e1;
     }
   }
   __syncthreads();
@@ -742,6 +796,10 @@ __device__ void op_dense_mma(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 }
 
 __device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   if (op.k & PGX_DENSE_MMA) {
     op_dense_mma(c, op, I);
     return;
@@ -752,9 +810,9 @@ __device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   zero_tail(c, y, rows);
-  for (int idx = c.tid; idx < c.tb * rows; idx += c.nthreads) {
-    int r = idx / c.tb, t = idx - r * c.tb;
-    const double* xl = x + t * c.lcap;
+  for (int idx = c_tid; idx < c_tb * rows; idx += c_nthreads) {
+    int r = idx / c_tb, t = idx - r * c_tb;
+    const double* xl = x + t * c_lcap;
     const double* Ar = A + (size_t)r * cols;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     int k = 0;
@@ -765,7 +823,7 @@ __device__ void op_dense(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       a3 = fma(__ldg(Ar + k + 3), xl[k + 3], a3);
     }
     for (; k < cols; ++k) a0 = fma(__ldg(Ar + k), xl[k], a0);
-    y[t * c.lcap + r] = (a0 + a1) + (a2 + a3);
+    y[t * c_lcap + r] = (a0 + a1) + (a2 + a3);
   }
   __syncthreads();
   swap_spare(c, op.a);
@@ -850,13 +908,18 @@ template <int R, bool FIRST, bool LAST>
 __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src, double2* dst, const double2* tw,
                                                int L, int Ns, int npairs, double* x, const DctScale& ds,
                                                int tws = 1) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_fft_stride = c.fft_stride;
   const int LR = L / R;
   const int step = tws * (L / (Ns * R));  // twiddle table holds exp(-2 pi i k / (tws L))
   const int N = L >> 1;
-  for (int idx = c.tid; idx < npairs * LR; idx += c.nthreads) {
+  for (int idx = c_tid; idx < npairs * LR; idx += c_nthreads) {
     int pr = idx / LR, j = idx - pr * LR;
     const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
+    const bool two = t0 + 1 < c_tb;
     int k = j % Ns;
     double2 v[R];
 #pragma unroll
@@ -864,15 +927,15 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
       const int m = j + r * LR;
       if (FIRST) {
         const int sidx = m <= N ? m : L - m;
-        double a = x[t0 * c.lcap + sidx];
-        double b = two ? x[(t0 + 1) * c.lcap + sidx] : 0.0;
+        double a = x[t0 * c_lcap + sidx];
+        double b = two ? x[(t0 + 1) * c_lcap + sidx] : 0.0;
         if (ds.has_pre) {
           a = ds.scale_pre(a, sidx, N);
           b = ds.scale_pre(b, sidx, N);
         }
         v[r] = make_double2(a, b);
       } else {
-        v[r] = src[pr * c.fft_stride + m];
+        v[r] = src[pr * c_fft_stride + m];
       }
     }
     double2 o[R];
@@ -931,11 +994,11 @@ __device__ __forceinline__ void stockham_stage(const Ctx& c, const double2* src,
             z.x *= sc;
             z.y *= sc;
           }
-          x[t0 * c.lcap + kk] = z.x;
-          if (two) x[(t0 + 1) * c.lcap + kk] = z.y;
+          x[t0 * c_lcap + kk] = z.x;
+          if (two) x[(t0 + 1) * c_lcap + kk] = z.y;
         }
       } else {
-        dst[pr * c.fft_stride + kk] = o[q];
+        dst[pr * c_fft_stride + kk] = o[q];
       }
     }
   }
@@ -1020,24 +1083,30 @@ __device__ __forceinline__ void butterfly_plain(double2* v, double2* o) {
 template <int R>
 __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const double2* tw, int N, int nall,
                                            int npairs, int slot0, const DctScale& ds) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_fft_stride = c.fft_stride;
   const int LR = N / R;
   const double* cmt = reinterpret_cast<const double*>(tw + 2 * N);
-  for (int idx = c.tid; idx < nall * LR; idx += c.nthreads) {
+  double* const x0s = slot_ptr(c, slot0);
+  for (int idx = c_tid; idx < nall * LR; idx += c_nthreads) {
     const int P = idx / LR, j = idx - P * LR;
     const int sl = P / npairs, pr = P - sl * npairs;
-    const double* x = slot_ptr(c, slot0 + sl);
+    const double* x = op_slot(c, x0s, slot0, sl);
     const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
+    const bool two = t0 + 1 < c_tb;
     double2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int m = j + r * LR;
       const double cm = __ldg(cmt + m);  // 1/2 - sin(pi m / N), after the 2N twiddles
-      const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
+      const double a0 = x[t0 * c_lcap + m], a1 = x[t0 * c_lcap + N - m];
       double ua = fma(cm, a0 - a1, a1);
       double ub = 0.0;
       if (two) {
-        const double b0 = x[(t0 + 1) * c.lcap + m], b1 = x[(t0 + 1) * c.lcap + N - m];
+        const double b0 = x[(t0 + 1) * c_lcap + m], b1 = x[(t0 + 1) * c_lcap + N - m];
         ub = fma(cm, b0 - b1, b1);
       }
       if (ds.has_pre) {
@@ -1049,7 +1118,7 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
     double2 o[R];
     butterfly_plain<R>(v, o);
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[P * c.fft_stride + j * R + q] = o[q];
+    for (int q = 0; q < R; ++q) dst[P * c_fft_stride + j * R + q] = o[q];
   }
 }
 
@@ -1067,28 +1136,35 @@ __device__ __forceinline__ void fold_stage(const Ctx& c, double2* dst, const dou
 // The backward pre-scale (-1)^j w_j is common to x_j and x_{N-j} (N even) and
 // applied to u_j, d_j; the forward post-scale to the outputs.
 __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_fft_stride = c.fft_stride;
+  double* const c_ybuf = c.ybuf;
   // op.b > 1: the transforms of slots a .. a+b-1 (same length and mode) go through every
   // phase together: one barrier per phase for all of them, b times the parallel work.
   const int ns = nslot_of(op);
+  double* const x0s = slot_ptr(c, op.a);
   const int n = c.slen[op.a];
   const int N = n - 1, H = N / 2;
   const int mode = op.k & PGX_DCT_MODE_MASK;
   const DctScale ds = dct_scale(mode, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
-  const int npairs = (c.tb + 1) >> 1;
+  const int npairs = (c_tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
   int rest = 1;
   const bool in_slot = (op.k & PGX_DCT_SLOT) != 0;
   const RadixPlan plan = in_slot ? odd_stages(radix_plan(N, rest)) : radix_plan(N, rest);
-  if (N > c.fft_stride || rest != 1 || plan.stages() < 1 || (in_slot && (ns != 1 || (c.tb & 1)))) {
+  if (N > c_fft_stride || rest != 1 || plan.stages() < 1 || (in_slot && (ns != 1 || (c_tb & 1)))) {
     // no buffer or plan for this length: refuse loudly
     for (int sl = 0; sl < ns; ++sl)
-      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+      for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) x_nan(c, op.a + sl, idx, n);
     return;
   }
   // y_1, L lanes a line, the op's lines spread over the warps (line lt = sl * tb + t); the j of a
   // lane keep one parity (L even), so the alternating pre-scale of BWD / FWD_T is one sign per lane
-  const int nlines = ns * c.tb;
+  const int nlines = ns * c_tb;
   const LineLanes g = line_lanes(c, nlines);
   {
     const bool alt = mode == PGX_DCT_BWD || mode == PGX_DCT_FWD_T;
@@ -1097,14 +1173,14 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
     for (int base = g.first; base < nlines; base += g.stride) {
       const int lt = base + g.grp;
       const bool valid = lt < nlines;
-      const int sl = valid ? lt / c.tb : 0, t = valid ? lt - sl * c.tb : 0;
-      const double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
+      const int sl = valid ? lt / c_tb : 0, t = valid ? lt - sl * c_tb : 0;
+      const double* xl = op_slot(c, x0s, op.a, sl) + t * c_lcap;
       double acc = 0.0;
       if (valid)
         for (int j = 1 + g.sub; j < H; j += g.L) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
       if (alt && ((1 + g.sub) & 1)) acc = -acc;
       for (int o = g.L >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, g.L);
-      if (valid && g.sub == 0) c.ybuf[lt] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
+      if (valid && g.sub == 0) c_ybuf[lt] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
     }
   }
   // FFT of length N over all pairs, the radix plan of the warp-local form (y_1 above and the first
@@ -1124,28 +1200,28 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
   __syncthreads();
   const double2* Z = bufs[cur];
   // untangle: even outputs, odd increments
-  for (int idx = c.tid; idx < nall * (H + 1); idx += c.nthreads) {
+  for (int idx = c_tid; idx < nall * (H + 1); idx += c_nthreads) {
     const int P = idx / (H + 1), m = idx - P * (H + 1);
     const int sl = P / npairs, pr = P - sl * npairs;
-    double* x = slot_ptr(c, op.a + sl);
+    double* x = op_slot(c, x0s, op.a, sl);
     const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
-    const double2 zm = Z[P * c.fft_stride + m];
-    const double2 zn = Z[P * c.fft_stride + (m == 0 ? 0 : N - m)];
+    const bool two = t0 + 1 < c_tb;
+    const double2 zm = Z[P * c_fft_stride + m];
+    const double2 zn = Z[P * c_fft_stride + (m == 0 ? 0 : N - m)];
     double ya = zm.x + zn.x, yb = zm.y + zn.y;
     if (ds.has_post) {
       const double sc = ds.post(2 * m, N);
       ya *= sc;
       yb *= sc;
     }
-    x[t0 * c.lcap + 2 * m] = ya;
-    if (two) x[(t0 + 1) * c.lcap + 2 * m] = yb;
+    x[t0 * c_lcap + 2 * m] = ya;
+    if (two) x[(t0 + 1) * c_lcap + 2 * m] = yb;
     if (m >= 1 && m < H) {
-      x[t0 * c.lcap + 2 * m + 1] = zn.y - zm.y;
-      if (two) x[(t0 + 1) * c.lcap + 2 * m + 1] = zm.x - zn.x;
+      x[t0 * c_lcap + 2 * m + 1] = zn.y - zm.y;
+      if (two) x[(t0 + 1) * c_lcap + 2 * m + 1] = zm.x - zn.x;
     } else if (m == 0) {
-      x[t0 * c.lcap + 1] = c.ybuf[sl * c.tb + t0];
-      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
+      x[t0 * c_lcap + 1] = c_ybuf[sl * c_tb + t0];
+      if (two) x[(t0 + 1) * c_lcap + 1] = c_ybuf[sl * c_tb + t0 + 1];
     }
   }
   if (in_slot) zero_tail(c, slot_ptr(c, op.a), n);  // the FFT stages wrote past the lines' ends
@@ -1157,8 +1233,8 @@ __device__ void op_dct_even_cta(Ctx& c, const pgx_op& op, const pgx_instance& I)
     for (int base = g.first; base < nlines; base += g.stride) {
       const int lt = base + g.grp;
       const bool valid = lt < nlines;
-      const int sl = valid ? lt / c.tb : 0, t = valid ? lt - sl * c.tb : 0;
-      double* xl = slot_ptr(c, op.a + sl) + t * c.lcap;
+      const int sl = valid ? lt / c_tb : 0, t = valid ? lt - sl * c_tb : 0;
+      double* xl = op_slot(c, x0s, op.a, sl) + t * c_lcap;
       const int m0 = min(g.sub * chunk, H), m1 = min(m0 + chunk, H);
       double run = 0.0;
       if (valid)
@@ -1210,25 +1286,29 @@ __device__ __forceinline__ WarpPairs warp_pairs(const Ctx& c, int nall) {
 template <int R>
 __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2* dst, const double2* tw, int N,
                                       int npairs, int slot0, const DctScale& ds) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_fft_stride = c.fft_stride;
   const int B = N / R;
   const double* cmt = reinterpret_cast<const double*>(tw + 2 * N);
+  double* const x0s = slot_ptr(c, slot0);
   for (int it = g.lane; it < g.npw * B; it += 32) {
     const int q = it / B, j = it - q * B;
     const int P = g.w + q * g.nw;
     const int sl = P / npairs, pr = P - sl * npairs;
-    const double* x = slot_ptr(c, slot0 + sl);
+    const double* x = op_slot(c, x0s, slot0, sl);
     const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
+    const bool two = t0 + 1 < c_tb;
     double2 v[R], o[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int m = j + r * B;
       const double cm = __ldg(cmt + m);  // 1/2 - sin(pi m / N), after the 2N twiddles
-      const double a0 = x[t0 * c.lcap + m], a1 = x[t0 * c.lcap + N - m];
+      const double a0 = x[t0 * c_lcap + m], a1 = x[t0 * c_lcap + N - m];
       double ua = fma(cm, a0 - a1, a1);
       double ub = 0.0;
       if (two) {
-        const double b0 = x[(t0 + 1) * c.lcap + m], b1 = x[(t0 + 1) * c.lcap + N - m];
+        const double b0 = x[(t0 + 1) * c_lcap + m], b1 = x[(t0 + 1) * c_lcap + N - m];
         ub = fma(cm, b0 - b1, b1);
       }
       if (ds.has_pre) {
@@ -1239,7 +1319,7 @@ __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2*
     }
     butterfly_plain<R>(v, o);
 #pragma unroll
-    for (int q2 = 0; q2 < R; ++q2) dst[P * c.fft_stride + j * R + q2] = o[q2];
+    for (int q2 = 0; q2 < R; ++q2) dst[P * c_fft_stride + j * R + q2] = o[q2];
   }
 }
 
@@ -1247,13 +1327,14 @@ __device__ __forceinline__ void wfold(const Ctx& c, const WarpPairs& g, double2*
 template <int R>
 __device__ __forceinline__ void wstage(const Ctx& c, const WarpPairs& g, const double2* src, double2* dst,
                                        const double2* tw, int L, int Ns, int tws) {
+  const int c_fft_stride = c.fft_stride;
   const int B = L / R;
   const int step = tws * (L / (Ns * R));
   for (int it = g.lane; it < g.npw * B; it += 32) {
     const int q = it / B, j = it - q * B;
     const int P = g.w + q * g.nw;
     const int k = j % Ns;
-    const double2* s = src + P * c.fft_stride;
+    const double2* s = src + P * c_fft_stride;
     double2 v[R], o[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[j + r * B];
@@ -1276,29 +1357,36 @@ __device__ __forceinline__ void wstage(const Ctx& c, const WarpPairs& g, const d
       }
       butterfly_plain<3>(v, o);
     }
-    double2* d = dst + P * c.fft_stride + (j - k) * R + k;
+    double2* d = dst + P * c_fft_stride + (j - k) * R + k;
 #pragma unroll
     for (int q2 = 0; q2 < R; ++q2) d[q2 * Ns] = o[q2];
   }
 }
 
 __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_fft_stride = c.fft_stride;
+  double* const c_ybuf = c.ybuf;
   const int ns = nslot_of(op);
+  double* const x0s = slot_ptr(c, op.a);
   const int n = c.slen[op.a];
   const int N = n - 1, H = N / 2;
   const int mode = op.k & PGX_DCT_MODE_MASK;
   const DctScale ds = dct_scale(mode, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
-  const int npairs = (c.tb + 1) >> 1;
+  const int npairs = (c_tb + 1) >> 1;
   const int nall = ns * npairs;  // line pairs of all slots; pair P = s * npairs + pr
   int rest = 1;
   const bool in_slot = (op.k & PGX_DCT_SLOT) != 0;
   const RadixPlan plan = radix_plan(N, rest);
-  if (N > c.fft_stride || rest != 1 || plan.stages() < 1 ||
-      (in_slot && (ns != 1 || (c.tb & 1) || odd_stages(plan).stages() < 1))) {
+  if (N > c_fft_stride || rest != 1 || plan.stages() < 1 ||
+      (in_slot && (ns != 1 || (c_tb & 1) || odd_stages(plan).stages() < 1))) {
     // no buffer or plan for this length: refuse loudly
     for (int sl = 0; sl < ns; ++sl)
-      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+      for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) x_nan(c, op.a + sl, idx, n);
     return;
   }
   const WarpPairs g = warp_pairs(c, nall);
@@ -1322,14 +1410,14 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       const int ll = base + grp, q = ll >> 1;
       const int P = g.w + q * g.nw;
       const int sl = P / npairs, t = 2 * (P - sl * npairs) + (ll & 1);
-      const bool valid = ll < nl && t < c.tb;
+      const bool valid = ll < nl && t < c_tb;
       double acc = 0.0;
-      const double* xl = slot_ptr(c, op.a + (valid ? sl : 0)) + (valid ? t : 0) * c.lcap;
+      const double* xl = op_slot(c, x0s, op.a, valid ? sl : 0) + (valid ? t : 0) * c_lcap;
       if (valid)
         for (int j = 1 + sub; j < H; j += L) acc = fma(__ldg(&tw[j].x), xl[j] - xl[N - j], acc);
       if (alt && ((1 + sub) & 1)) acc = -acc;
       for (int o = L >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, L);
-      if (valid && sub == 0) c.ybuf[sl * c.tb + t] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
+      if (valid && sub == 0) c_ybuf[sl * c_tb + t] = fma(2.0 * ps, acc, (xl[0] - xl[N]) * p0);
     }
   }
   // FFT of length N over the warp's pairs, ping-pong between the two buffers
@@ -1355,34 +1443,34 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
     const int q = it / (H + 1), m = it - q * (H + 1);
     const int P = g.w + q * g.nw;
     const int sl = P / npairs, pr = P - sl * npairs;
-    double* x = slot_ptr(c, op.a + sl);
+    double* x = op_slot(c, x0s, op.a, sl);
     const int t0 = 2 * pr;
-    const bool two = t0 + 1 < c.tb;
-    const double2 zm = Z[P * c.fft_stride + m];
-    const double2 zn = Z[P * c.fft_stride + (m == 0 ? 0 : N - m)];
+    const bool two = t0 + 1 < c_tb;
+    const double2 zm = Z[P * c_fft_stride + m];
+    const double2 zn = Z[P * c_fft_stride + (m == 0 ? 0 : N - m)];
     double ya = zm.x + zn.x, yb = zm.y + zn.y;
     if (ds.has_post) {
       const double sc = ds.post(2 * m, N);
       ya *= sc;
       yb *= sc;
     }
-    x[t0 * c.lcap + 2 * m] = ya;
-    if (two) x[(t0 + 1) * c.lcap + 2 * m] = yb;
+    x[t0 * c_lcap + 2 * m] = ya;
+    if (two) x[(t0 + 1) * c_lcap + 2 * m] = yb;
     if (m >= 1 && m < H) {
-      x[t0 * c.lcap + 2 * m + 1] = zn.y - zm.y;
-      if (two) x[(t0 + 1) * c.lcap + 2 * m + 1] = zm.x - zn.x;
+      x[t0 * c_lcap + 2 * m + 1] = zn.y - zm.y;
+      if (two) x[(t0 + 1) * c_lcap + 2 * m + 1] = zm.x - zn.x;
     } else if (m == 0) {
-      x[t0 * c.lcap + 1] = c.ybuf[sl * c.tb + t0];
-      if (two) x[(t0 + 1) * c.lcap + 1] = c.ybuf[sl * c.tb + t0 + 1];
+      x[t0 * c_lcap + 1] = c_ybuf[sl * c_tb + t0];
+      if (two) x[(t0 + 1) * c_lcap + 1] = c_ybuf[sl * c_tb + t0 + 1];
     }
   }
   if (in_slot) {  // the FFT stages wrote past the ends of the warp's lines: zero [n, lcap) again
-    const int w = c.lcap - n;
+    const int w = c_lcap - n;
     double* x = slot_ptr(c, op.a);
     for (int it = g.lane; it < g.npw * 2 * w; it += 32) {
       const int q = it / (2 * w), r = it - q * 2 * w;
       const int t = 2 * (g.w + q * g.nw) + (r >= w ? 1 : 0);  // one slot: pair P = line pair P
-      x[t * c.lcap + n + (r >= w ? r - w : r)] = 0.0;
+      x[t * c_lcap + n + (r >= w ? r - w : r)] = 0.0;
     }
   }
   __syncwarp();
@@ -1394,8 +1482,8 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       const int ll = base + grp, q = ll >> 1;
       const int P = g.w + q * g.nw;
       const int sl = P / npairs, t = 2 * (P - sl * npairs) + (ll & 1);
-      const bool valid = ll < nl && t < c.tb;
-      double* xl = slot_ptr(c, op.a + (valid ? sl : 0)) + (valid ? t : 0) * c.lcap;
+      const bool valid = ll < nl && t < c_tb;
+      double* xl = op_slot(c, x0s, op.a, valid ? sl : 0) + (valid ? t : 0) * c_lcap;
       const int m0 = min(sub * chunk, H), m1 = min(m0 + chunk, H);
       double run = 0.0;
       if (valid)
@@ -1427,19 +1515,22 @@ __device__ void op_dct_even(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_instance& I);
 
 __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
   const int n = c.slen[op.a];
   if (((n - 1) & 1) == 0 && n >= 3) {
     // a tile with fewer line pairs per slot than warps (single instances, short passes) leaves
     // warps idle in the warp-local form; there the CTA-wide form spreads each pair over all warps
     // (per slot, so a multi-slot op and its one-op-per-slot split take the same form)
-    if ((op.k & PGX_DCT_CTA) || ((c.tb + 1) >> 1) < (c.nthreads >> 5)) op_dct_even_cta(c, op, I);
+    if ((op.k & PGX_DCT_CTA) || ((c_tb + 1) >> 1) < (c_nthreads >> 5)) op_dct_even_cta(c, op, I);
     else op_dct_even(c, op, I);
     return;
   }
   const int ns = nslot_of(op);  // paired-line path: one slot after the other
   if (op.k & PGX_DCT_SLOT) {  // needs 2(n - 1) complex values a pair: no room in the slot, refuse loudly
     for (int sl = 0; sl < ns; ++sl)
-      for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, op.a + sl, idx, n);
+      for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) x_nan(c, op.a + sl, idx, n);
     return;
   }
   for (int sl = 0; sl < ns; ++sl) {
@@ -1449,16 +1540,21 @@ __device__ void op_dct(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 }
 
 __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_instance& I) {
+  const int c_tb = c.tb;
+  const int c_lcap = c.lcap;
+  const int c_nthreads = c.nthreads;
+  const int c_tid = c.tid;
+  const int c_fft_stride = c.fft_stride;
   const int n = c.slen[slot];
-  if (2 * (n - 1) > c.fft_stride) {  // buffer sized for a shorter even length: refuse loudly
-    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) x_nan(c, slot, idx, n);
+  if (2 * (n - 1) > c_fft_stride) {  // buffer sized for a shorter even length: refuse loudly
+    for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) x_nan(c, slot, idx, n);
     return;
   }
   const int N = n - 1, L = 2 * N;
   const DctScale ds = dct_scale(op.k & PGX_DCT_MODE_MASK, N);
   const double2* tw = reinterpret_cast<const double2*>(I.mat[op.mat]);
   double* x = slot_ptr(c, slot);
-  const int npairs = (c.tb + 1) >> 1;
+  const int npairs = (c_tb + 1) >> 1;
   int nst = 0;
   for (int rem = L; rem > 1; rem /= next_radix(rem)) ++nst;
   double2* bufs[2] = {c.f0, c.f1};
@@ -1489,12 +1585,12 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
     __syncthreads();
   }
   if (nst == 1) {  // tiny transform: copy the single stage's output back
-    for (int idx = c.tid; idx < c.tb * n; idx += c.nthreads) {
+    for (int idx = c_tid; idx < c_tb * n; idx += c_nthreads) {
       int t = idx / n, k = idx - t * n;
-      double2 z = c.f0[(t >> 1) * c.fft_stride + k];
+      double2 z = c.f0[(t >> 1) * c_fft_stride + k];
       double y = (t & 1) ? z.y : z.x;
       if (ds.has_post) y *= ds.post(k, N);
-      x[t * c.lcap + k] = y;
+      x[t * c_lcap + k] = y;
     }
   }
 }
