@@ -166,22 +166,38 @@ __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axi
   double* s = slot_ptr(c, op.a);
   const int tb = c_tb;
   const bool contig = (v.se == 1);
-  for (int idx = c_tid; idx < tb * n; idx += c_nthreads) {
-    int t, i;
-    if (contig) { t = idx / n; i = idx - t * n; }
-    else { i = idx / tb; t = idx - i * tb; }
-    const int line = c_l0 + t;
-    double x = 0.0;
-    if (i < v.ne && line < v.nl && line < c_nlines) x = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
-    double* d = s + t * c_lcap + i;
-    if (mode == 0) *d = alpha == 1.0 ? x : alpha * x;
-    else if (mode == 1) *d = fma(alpha, x, *d);
-    else *d = (alpha == 1.0 ? x : alpha * x) * (*d);
+  const int total = tb * n;
+  // up to kU elements a thread per round, all their global loads issued before the first store to
+  // the slot: the stores go through generic pointers, which the compiler may not move loads across,
+  // so one element at a time would wait out a full memory latency per element
+  constexpr int kU = 4;
+  for (int base = c_tid; base < total; base += kU * c_nthreads) {
+    double x[kU];
+    int off[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int idx = base + u * c_nthreads;
+      x[u] = 0.0;
+      off[u] = -1;
+      if (idx < total) {
+        int t, i;
+        if (contig) { t = idx / n; i = idx - t * n; }
+        else { i = idx / tb; t = idx - i * tb; }
+        const int line = c_l0 + t;
+        off[u] = t * c_lcap + i;
+        if (i < v.ne && line < v.nl && line < c_nlines) x[u] = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (off[u] < 0) continue;
+      double* d = s + off[u];
+      if (mode == 0) *d = alpha == 1.0 ? x[u] : alpha * x[u];
+      else if (mode == 1) *d = fma(alpha, x[u], *d);
+      else *d = (alpha == 1.0 ? x[u] : alpha * x[u]) * (*d);
+    }
   }
-  if (mode == 0) {
-    __syncthreads();
-    zero_tail(c, s, n);
-  }
+  if (mode == 0) zero_tail(c, s, n);  // [n, lcap) of every line: no element the loop writes
 }
 
 __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, bool add) {
