@@ -213,16 +213,36 @@ __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, 
   const int n = v.ne;
   const int tb = c_tb;
   const bool contig = (v.se == 1);
-  for (int idx = c_tid; idx < tb * n; idx += c_nthreads) {
-    int t, i;
-    if (contig) { t = idx / n; i = idx - t * n; }
-    else { i = idx / tb; t = idx - i * tb; }
-    const int line = c_l0 + t;
-    if (line >= v.nl || line >= c_nlines) continue;
-    double x = s[t * c_lcap + i];
-    double* d = v.p + (int64_t)i * v.se + (int64_t)line * v.sl;
-    if (add) *d = fma(alpha, x, *d);
-    else *d = alpha == 1.0 ? x : alpha * x;
+  const int total = tb * n;
+  // up to kU elements a thread per round, every load (the slot's and, to accumulate, the array's)
+  // before the first store: one memory latency per round, not per element
+  constexpr int kU = 4;
+  for (int base = c_tid; base < total; base += kU * c_nthreads) {
+    double x[kU], old[kU];
+    double* dp[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int idx = base + u * c_nthreads;
+      dp[u] = nullptr;
+      x[u] = old[u] = 0.0;
+      if (idx < total) {
+        int t, i;
+        if (contig) { t = idx / n; i = idx - t * n; }
+        else { i = idx / tb; t = idx - i * tb; }
+        const int line = c_l0 + t;
+        if (line < v.nl && line < c_nlines) {
+          x[u] = s[t * c_lcap + i];
+          dp[u] = v.p + (int64_t)i * v.se + (int64_t)line * v.sl;
+          if (add) old[u] = *dp[u];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (!dp[u]) continue;
+      if (add) *dp[u] = fma(alpha, x[u], old[u]);
+      else *dp[u] = alpha == 1.0 ? x[u] : alpha * x[u];
+    }
   }
 }
 
@@ -252,10 +272,7 @@ __device__ void op_pointwise(Ctx& c, const pgx_op& op, const pgx_instance& I) {
       case PGX_OP_COPY: a[o] = alpha == 1.0 ? b[o] : alpha * b[o]; break;
     }
   }
-  if (op.code == PGX_OP_COPY) {
-    __syncthreads();
-    zero_tail(c, a, n);
-  }
+  if (op.code == PGX_OP_COPY) zero_tail(c, a, n);  // [n, lcap): no element the loop reads or writes
 }
 
 __device__ void op_setlen(Ctx& c, const pgx_op& op, const pgx_instance& I) {
@@ -276,15 +293,26 @@ __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   const int M = c.slen[op.a], N = M + 2;
-  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
-    int t = idx / c_lcap, i = idx - t * c_lcap;
-    double r = 0.0;
-    if (i < N) {
-      const double* xl = x + t * c_lcap;
-      r = i < M ? xl[i] : 0.0;
-      if (i >= 2) r = fma(__ldg(sd + i - 2), xl[i - 2], r);
+  const int total = c_tb * c_lcap;
+  constexpr int kU = 4;  // the table loads of kU elements before their stores
+  for (int base = c_tid; base < total; base += kU * c_nthreads) {
+    double r[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int idx = base + u * c_nthreads;
+      r[u] = 0.0;
+      if (idx < total) {
+        const int t = idx / c_lcap, i = idx - t * c_lcap;
+        if (i < N) {
+          const double* xl = x + t * c_lcap;
+          r[u] = i < M ? xl[i] : 0.0;
+          if (i >= 2) r[u] = fma(__ldg(sd + i - 2), xl[i - 2], r[u]);
+        }
+      }
     }
-    y[idx] = r;
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+      if (base + u * c_nthreads < total) y[base + u * c_nthreads] = r[u];
   }
   swap_spare(c, op.a);
   c.slen[op.a] = N;
@@ -300,14 +328,25 @@ __device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   const int N = c.slen[op.a], M = N - 2;
-  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
-    int t = idx / c_lcap, i = idx - t * c_lcap;
-    double r = 0.0;
-    if (i < M) {
-      const double* xl = x + t * c_lcap;
-      r = fma(__ldg(sd + i), xl[i + 2], xl[i]);
+  const int total = c_tb * c_lcap;
+  constexpr int kU = 4;  // the table loads of kU elements before their stores
+  for (int base = c_tid; base < total; base += kU * c_nthreads) {
+    double r[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int idx = base + u * c_nthreads;
+      r[u] = 0.0;
+      if (idx < total) {
+        const int t = idx / c_lcap, i = idx - t * c_lcap;
+        if (i < M) {
+          const double* xl = x + t * c_lcap;
+          r[u] = fma(__ldg(sd + i), xl[i + 2], xl[i]);
+        }
+      }
     }
-    y[idx] = r;
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+      if (base + u * c_nthreads < total) y[base + u * c_nthreads] = r[u];
   }
   swap_spare(c, op.a);
   c.slen[op.a] = M;
@@ -741,17 +780,28 @@ __device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int cols = c.slen[op.a];
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
-  for (int idx = c_tid; idx < c_tb * c_lcap; idx += c_nthreads) {
-    int t = idx / c_lcap, r = idx - t * c_lcap;
-    double acc = 0.0;
-    if (r < rows) {
-      const double* xl = x + t * c_lcap;
-      for (int d = 0; d < nd; ++d) {
-        int col = r + off0 + 2 * d;
-        if (col >= 0 && col < cols) acc = fma(__ldg(A + d * rows + r), xl[col], acc);
+  const int total = c_tb * c_lcap;
+  constexpr int kU = 2;  // the matrix loads of kU rows before their stores
+  for (int base = c_tid; base < total; base += kU * c_nthreads) {
+    double acc[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int idx = base + u * c_nthreads;
+      acc[u] = 0.0;
+      if (idx < total) {
+        const int t = idx / c_lcap, r = idx - t * c_lcap;
+        if (r < rows) {
+          const double* xl = x + t * c_lcap;
+          for (int d = 0; d < nd; ++d) {
+            const int col = r + off0 + 2 * d;
+            if (col >= 0 && col < cols) acc[u] = fma(__ldg(A + d * rows + r), xl[col], acc[u]);
+          }
+        }
       }
     }
-    y[idx] = acc;
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+      if (base + u * c_nthreads < total) y[base + u * c_nthreads] = acc[u];
   }
   swap_spare(c, op.a);
   c.slen[op.a] = rows;
