@@ -147,6 +147,7 @@ __device__ void zero_tail(const Ctx& c, double* b, int from) {
 
 // ------------------------------------------------------------------ load/store
 // mode 0: slot = alpha*arr (length n, zero beyond the array), 1: +=, 2: *=
+template <int KU>
 __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, int mode) {
   const int c_tb = c.tb;
   const int c_lcap = c.lcap;
@@ -169,8 +170,25 @@ __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axi
   const int total = tb * n;
   // up to kU elements a thread per round, all their global loads issued before the first store to
   // the slot: the stores go through generic pointers, which the compiler may not move loads across,
-  // so one element at a time would wait out a full memory latency per element
-  constexpr int kU = 4;
+  // so one element at a time would wait out a full memory latency per element (the build for
+  // launches of fewer CTAs than SMs, KU = 1, keeps the shorter single-element loop)
+  constexpr int kU = KU;
+  if (total <= c_nthreads) {  // at most one element a thread (single instances, short lines)
+    if (c_tid < total) {
+      int t, i;
+      if (contig) { t = c_tid / n; i = c_tid - t * n; }
+      else { i = c_tid / tb; t = c_tid - i * tb; }
+      const int line = c_l0 + t;
+      double x = 0.0;
+      if (i < v.ne && line < v.nl && line < c_nlines) x = v.p[(int64_t)i * v.se + (int64_t)line * v.sl];
+      double* d = s + t * c_lcap + i;
+      if (mode == 0) *d = alpha == 1.0 ? x : alpha * x;
+      else if (mode == 1) *d = fma(alpha, x, *d);
+      else *d = (alpha == 1.0 ? x : alpha * x) * (*d);
+    }
+    if (mode == 0) zero_tail(c, s, n);
+    return;
+  }
   for (int base = c_tid; base < total; base += kU * c_nthreads) {
     double x[kU];
     int off[kU];
@@ -200,6 +218,7 @@ __device__ void op_load(Ctx& c, const pgx_op& op, const pgx_instance& I, int axi
   if (mode == 0) zero_tail(c, s, n);  // [n, lcap) of every line: no element the loop writes
 }
 
+template <int KU>
 __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, int axis, bool add) {
   const int c_tb = c.tb;
   const int c_lcap = c.lcap;
@@ -216,7 +235,22 @@ __device__ void op_store(const Ctx& c, const pgx_op& op, const pgx_instance& I, 
   const int total = tb * n;
   // up to kU elements a thread per round, every load (the slot's and, to accumulate, the array's)
   // before the first store: one memory latency per round, not per element
-  constexpr int kU = 4;
+  constexpr int kU = KU;
+  if (total <= c_nthreads) {  // at most one element a thread (single instances, short lines)
+    if (c_tid < total) {
+      int t, i;
+      if (contig) { t = c_tid / n; i = c_tid - t * n; }
+      else { i = c_tid / tb; t = c_tid - i * tb; }
+      const int line = c_l0 + t;
+      if (line < v.nl && line < c_nlines) {
+        const double x = s[t * c_lcap + i];
+        double* d = v.p + (int64_t)i * v.se + (int64_t)line * v.sl;
+        if (add) *d = fma(alpha, x, *d);
+        else *d = alpha == 1.0 ? x : alpha * x;
+      }
+    }
+    return;
+  }
   for (int base = c_tid; base < total; base += kU * c_nthreads) {
     double x[kU], old[kU];
     double* dp[kU];
@@ -284,6 +318,7 @@ __device__ void op_setlen(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 
 // ------------------------------------------------------------------ stencils
 // u_i = v_i [i < M] + s_{i-2} v_{i-2} [i >= 2],  s = S[i+2, i] sub-diagonal table.
+template <int KU>
 __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int c_tb = c.tb;
   const int c_lcap = c.lcap;
@@ -294,7 +329,7 @@ __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   double* y = spare_ptr(c);
   const int M = c.slen[op.a], N = M + 2;
   const int total = c_tb * c_lcap;
-  constexpr int kU = 4;  // the table loads of kU elements before their stores
+  constexpr int kU = KU;  // the table loads of kU elements before their stores
   for (int base = c_tid; base < total; base += kU * c_nthreads) {
     double r[kU];
 #pragma unroll
@@ -319,6 +354,7 @@ __device__ void op_stencil(Ctx& c, const pgx_op& op, const pgx_instance& I) {
 }
 
 // (S^T u)_i = u_i + s_i u_{i+2},  i < N-2.
+template <int KU>
 __device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int c_tb = c.tb;
   const int c_lcap = c.lcap;
@@ -329,7 +365,7 @@ __device__ void op_stencil_t(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   double* y = spare_ptr(c);
   const int N = c.slen[op.a], M = N - 2;
   const int total = c_tb * c_lcap;
-  constexpr int kU = 4;  // the table loads of kU elements before their stores
+  constexpr int kU = KU;  // the table loads of kU elements before their stores
   for (int base = c_tid; base < total; base += kU * c_nthreads) {
     double r[kU];
 #pragma unroll
@@ -769,6 +805,7 @@ __device__ void op_fdma(Ctx& c, const pgx_op& op, const pgx_instance& I, bool pe
 }
 
 // --------------------------------------------------------- banded / dense
+template <int KU>
 __device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const int c_tb = c.tb;
   const int c_lcap = c.lcap;
@@ -781,7 +818,7 @@ __device__ void op_banded(Ctx& c, const pgx_op& op, const pgx_instance& I) {
   const double* x = slot_ptr(c, op.a);
   double* y = spare_ptr(c);
   const int total = c_tb * c_lcap;
-  constexpr int kU = 2;  // the matrix loads of kU rows before their stores
+  constexpr int kU = KU > 2 ? 2 : KU;  // the matrix loads of kU rows before their stores
   for (int base = c_tid; base < total; base += kU * c_nthreads) {
     double acc[kU];
 #pragma unroll
@@ -1663,7 +1700,7 @@ __device__ void dct_paired_slot(Ctx& c, int slot, const pgx_op& op, const pgx_in
 
 // ------------------------------------------------------------------ driver
 // One tile of one instance: the program's ops on shared-memory slots that start at `sm`.
-template <bool FFT>
+template <bool FFT, int KU>
 __device__ void run_program(const pgx_program& P, const pgx_instance& I, int tile, double* sm) {
   Ctx c;
   c.tb = P.tb;
@@ -1695,18 +1732,18 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   for (int o = 0; o < P.nops; ++o) {
     const pgx_op& op = P.ops[o];
     switch (op.code) {
-      case PGX_OP_LOAD: op_load(c, op, I, P.axis, 0); break;
-      case PGX_OP_LOAD_ADD: op_load(c, op, I, P.axis, 1); break;
-      case PGX_OP_LOAD_MUL: op_load(c, op, I, P.axis, 2); break;
-      case PGX_OP_STORE: op_store(c, op, I, P.axis, false); break;
-      case PGX_OP_STORE_ADD: op_store(c, op, I, P.axis, true); break;
+      case PGX_OP_LOAD: op_load<KU>(c, op, I, P.axis, 0); break;
+      case PGX_OP_LOAD_ADD: op_load<KU>(c, op, I, P.axis, 1); break;
+      case PGX_OP_LOAD_MUL: op_load<KU>(c, op, I, P.axis, 2); break;
+      case PGX_OP_STORE: op_store<KU>(c, op, I, P.axis, false); break;
+      case PGX_OP_STORE_ADD: op_store<KU>(c, op, I, P.axis, true); break;
       case PGX_OP_SCALE:
       case PGX_OP_AXPY:
       case PGX_OP_MUL:
       case PGX_OP_COPY: op_pointwise(c, op, I); break;
       case PGX_OP_SETLEN: op_setlen(c, op, I); break;
-      case PGX_OP_STENCIL: op_stencil(c, op, I); break;
-      case PGX_OP_STENCIL_T: op_stencil_t(c, op, I); break;
+      case PGX_OP_STENCIL: op_stencil<KU>(c, op, I); break;
+      case PGX_OP_STENCIL_T: op_stencil_t<KU>(c, op, I); break;
       case PGX_OP_TDMA2: op_tdma2(c, op, I); break;
       case PGX_OP_DIFF: op_diff(c, op); break;
       case PGX_OP_DCT:
@@ -1723,7 +1760,7 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
           op_dct(c, op, I);
         }
         break;
-      case PGX_OP_BANDED: op_banded(c, op, I); break;
+      case PGX_OP_BANDED: op_banded<KU>(c, op, I); break;
       case PGX_OP_DENSE: op_dense(c, op, I); break;
       case PGX_OP_FDMA: op_fdma(c, op, I, false); break;
       case PGX_OP_POISSON: op_fdma(c, op, I, true); break;
@@ -1739,7 +1776,7 @@ __device__ void run_program(const pgx_program& P, const pgx_instance& I, int til
   }
 }
 
-template <bool FFT>
+template <bool FFT, int KU>
 __device__ __forceinline__ void run_batched(const pgx_program& P, const pgx_instance* __restrict__ insts,
                                             const int32_t* __restrict__ work) {
   extern __shared__ __align__(16) double smem_dyn[];
@@ -1750,7 +1787,7 @@ __device__ __forceinline__ void run_batched(const pgx_program& P, const pgx_inst
   double* dst = reinterpret_cast<double*>(sI);
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
   __syncthreads();
-  run_program<FFT>(P, *sI, tile, smem_dyn + (sizeof(pgx_instance) + 7) / 8);
+  run_program<FFT, KU>(P, *sI, tile, smem_dyn + (sizeof(pgx_instance) + 7) / 8);
 }
 
 // ------------------------------------------------------------- persistent steps
@@ -1824,7 +1861,7 @@ __global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_persistent(
       for (int i = threadIdx.x; i < words; i += blockDim.x) pd[i] = ps[i];
     }
     __syncthreads();
-    run_program<true>(*sP, *sI, w.tile, slots);
+    run_program<true, 4>(*sP, *sI, w.tile, slots);
     // run_program ends every op with a block barrier: every store of the tile is done here
     if (threadIdx.x == 0) {
       __threadfence();
@@ -1838,24 +1875,38 @@ __global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_persistent(
 __global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_single(const __grid_constant__ pgx_program P,
                                                                        const __grid_constant__ pgx_instance I) {
   extern __shared__ __align__(16) double smem_dyn[];
-  run_program<false>(P, I, blockIdx.x, smem_dyn);
+  run_program<false, 1>(P, I, blockIdx.x, smem_dyn);
 }
 
 __global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_single_fft(const __grid_constant__ pgx_program P,
                                                                                const __grid_constant__ pgx_instance I) {
   extern __shared__ __align__(16) double smem_dyn[];
-  run_program<true>(P, I, blockIdx.x, smem_dyn);
+  run_program<true, 1>(P, I, blockIdx.x, smem_dyn);
 }
 
 __global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_batched(const __grid_constant__ pgx_program P,
                                                                         const pgx_instance* __restrict__ insts,
                                                                         const int32_t* __restrict__ work) {
-  run_batched<false>(P, insts, work);
+  run_batched<false, 4>(P, insts, work);
 }
 
 __global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_batched_fft(
     const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts, const int32_t* __restrict__ work) {
-  run_batched<true>(P, insts, work);
+  run_batched<true, 4>(P, insts, work);
+}
+
+// The same builds for launches of fewer CTAs than the GPU has SMs (single instances): each CTA's
+// ops are one latency chain with nothing to overlap, and the loops that batch several elements'
+// loads a thread cost there more than they hide.
+__global__ void __launch_bounds__(PGX_MAX_THREADS) line_program_batched_lat(const __grid_constant__ pgx_program P,
+                                                                            const pgx_instance* __restrict__ insts,
+                                                                            const int32_t* __restrict__ work) {
+  run_batched<false, 1>(P, insts, work);
+}
+
+__global__ void __launch_bounds__(PGX_MAX_THREADS_FFT) line_program_batched_fft_lat(
+    const __grid_constant__ pgx_program P, const pgx_instance* __restrict__ insts, const int32_t* __restrict__ work) {
+  run_batched<true, 1>(P, insts, work);
 }
 
 }  // namespace pgx
@@ -1881,7 +1932,7 @@ namespace pgx {
 // could invalidate by setting a lower value.
 static int raise_smem_cap_once(const void* fn, int which) {
   static std::mutex mu;
-  static bool done[5][64] = {};
+  static bool done[7][64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
@@ -1955,17 +2006,38 @@ int launch_persistent(const pgx_program* d_progs, int nprogs, const pgx_instance
   return (int)cudaGetLastError();
 }
 
+// SMs of the current device, looked up once per device.
+static int sm_count() {
+  static std::mutex mu;
+  static int count[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  std::lock_guard<std::mutex> lk(mu);
+  if (count[dev] == 0 && cudaDeviceGetAttribute(&count[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    count[dev] = 0;
+  }
+  return count[dev];
+}
+
 int launch_batched(const pgx_program* P, const pgx_instance* d_insts, const int32_t* d_work, int nwork,
                    cudaStream_t s) {
   int64_t smem = pgx_program_smem(P) + ((sizeof(pgx_instance) + 15) / 16) * 16;
   const bool fft = pgx_has_dct(*P);
+  const bool lat = nwork < sm_count();  // fewer CTAs than SMs: the latency build
+  const void* fn = fft ? (lat ? (const void*)line_program_batched_fft_lat : (const void*)line_program_batched_fft)
+                       : (lat ? (const void*)line_program_batched_lat : (const void*)line_program_batched);
   if (smem > 48 * 1024) {
-    int e = fft ? raise_smem_cap((const void*)line_program_batched_fft, 3)
-                : raise_smem_cap((const void*)line_program_batched, 1);
+    int e = raise_smem_cap(fn, fft ? (lat ? 6 : 3) : (lat ? 5 : 1));
     if (e) return e;
   }
-  if (fft) line_program_batched_fft<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
-  else line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  if (fft) {
+    if (lat) line_program_batched_fft_lat<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+    else line_program_batched_fft<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  } else {
+    if (lat) line_program_batched_lat<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+    else line_program_batched<<<nwork, P->nthreads, smem, s>>>(*P, d_insts, d_work);
+  }
   return (int)cudaGetLastError();
 }
 }  // namespace pgx
