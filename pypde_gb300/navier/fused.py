@@ -1059,8 +1059,16 @@ class FusedBatch:
         # explicit diffusion (beta != 1) in any instance: the batch runs the passes that carry it
         # (instances with beta = 1 add zero)
         self.beta = any(float(ns.beta) != 1.0 for ns in self.solvers)
-        self.insts, off, aoff = [], 0, 0
-        for ns, sh, ash in zip(self.solvers, shapes, ashapes):
+        # the states lie in the arena grouped by instance shape (the instances keep the caller's order):
+        # a host-memory pipeline group of one shape is one contiguous copy each way and launches one
+        # size class per pass
+        order = sorted(range(len(self.solvers)), key=lambda k: tuple(self.solvers[k].shape))
+        soff, off = [0] * len(self.solvers), 0
+        for k in order:
+            soff[k] = off
+            off += sum(r * c for (r, c) in shapes[k].values())
+        self.insts, aoff = [], 0
+        for ns, sh, ash, off in zip(self.solvers, shapes, ashapes, soff):
             views = {}
             for key in _Instance.STATE:
                 r, c = sh[key]
@@ -1400,20 +1408,34 @@ class FusedBatch:
         torch.cuda.synchronize()
         return times
 
-    def _split_groups(self, groups):
-        """[(instance indices, first, end offset in state_arena)]: up to ``groups`` contiguous groups
-        of instances of about equal state size."""
+    def _arena_order(self):
+        """(instance indices in the order their states lie in ``state_arena``, their start offsets
+        in that order followed by the arena's end)."""
         base = self.state_arena.data_ptr()
-        starts = [(I.arrays["UG"].data_ptr() - base) // 8 for I in self.insts] + [self.state_arena.numel()]
-        cum = np.cumsum(np.diff(starts))
-        cuts = [0] + [int(np.searchsorted(cum, cum[-1] * g / groups)) + 1 for g in range(1, groups)] + [len(cum)]
-        cuts = sorted(set(min(max(c, 0), len(cum)) for c in cuts))
-        return [(range(a, b), starts[a], starts[b]) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+        starts = [(I.arrays["UG"].data_ptr() - base) // 8 for I in self.insts]
+        order = sorted(range(len(self.insts)), key=lambda k: starts[k])
+        return order, [starts[k] for k in order] + [self.state_arena.numel()]
+
+    def _split_groups(self, groups):
+        """[(instance indices, first, end offset in state_arena)]: up to ``groups`` groups of
+        instances contiguous in the arena and of about equal state size; ``groups`` = "shape": one
+        group per instance shape (contiguous: the arena is laid out by shape)."""
+        order, starts = self._arena_order()
+        if groups == "shape":
+            cuts = [0] + [j for j in range(1, len(order))
+                          if (self.insts[order[j]].N, self.insts[order[j]].M)
+                          != (self.insts[order[j - 1]].N, self.insts[order[j - 1]].M)] + [len(order)]
+        else:
+            cum = np.cumsum(np.diff(starts))
+            cuts = [0] + [int(np.searchsorted(cum, cum[-1] * g / groups)) + 1 for g in range(1, groups)] + [len(cum)]
+            cuts = sorted(set(min(max(c, 0), len(cum)) for c in cuts))
+        return [(order[a:b], starts[a], starts[b]) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
 
     def host_pipeline(self, groups=2, branches="shape"):
-        """Prepare ``step_host``: the instances in ``groups`` contiguous groups of about equal state
-        size, each with its own launch set, CUDA graph (``branches``: its graph branches, as in
-        ``capture``) and stream."""
+        """Prepare ``step_host``: the instances in ``groups`` groups contiguous in the state arena, of
+        about equal state size (``groups`` = "shape": one group per instance shape), each with its
+        own launch set, CUDA graph (``branches``: its graph branches, as in ``capture``) and
+        stream."""
         self._pipe = []
         for idx, o0, o1 in self._split_groups(groups):
             sub = self._subset(idx)

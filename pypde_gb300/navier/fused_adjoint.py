@@ -409,14 +409,8 @@ class FusedAdjoint(FusedBatch):
     def __init__(self, solvers, split=None):
         FusedBatch.__init__(self, solvers, split=split)
         self.bar_arena = torch.zeros_like(self.state_arena)
-        off = 0
-        for I in self.insts:
-            views = {}
-            for key in _Instance.STATE:
-                r, c = I.arrays[key].shape
-                views["b" + key] = self.bar_arena[off:off + r * c].view(r, c)
-                off += r * c
-            add_adjoint_buffers(I, views, self.beta)
+        for I, d in zip(self.insts, self.views(self.bar_arena, keys=_Instance.STATE)):
+            add_adjoint_buffers(I, {"b" + key: v for key, v in d.items()}, self.beta)
         tkind = self.solvers[0].T.xs[0].id
         self.aprogs = build_adjoint_programs(tkind, self.fft, self.split, self.beta, rk3=self.nstage == 3)
         # per stage (RK3: its parameters, ADI tables and carried velocity gradients)
@@ -496,14 +490,14 @@ class FusedAdjoint(FusedBatch):
 
     # -- views of the per-instance state in the arenas
     def views(self, arena, keys=("UG", "VG", "TG")):
-        out, off = [], 0
+        """Per instance, views of ``keys`` into ``arena``, a tensor with the layout of ``state_arena``."""
+        base, out = self.state_arena.data_ptr(), []
         for I in self.insts:
             d = {}
-            for key in _Instance.STATE:
+            for key in keys:
                 r, c = I.arrays[key].shape
-                if key in keys:
-                    d[key] = arena[off:off + r * c].view(r, c)
-                off += r * c
+                off = (I.arrays[key].data_ptr() - base) // 8
+                d[key] = arena[off:off + r * c].view(r, c)
             out.append(d)
         return out
 
