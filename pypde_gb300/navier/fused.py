@@ -1431,7 +1431,7 @@ class FusedBatch:
             cuts = sorted(set(min(max(c, 0), len(cum)) for c in cuts))
         return [(order[a:b], starts[a], starts[b]) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
 
-    def host_pipeline(self, groups=2, branches="shape"):
+    def host_pipeline(self, groups="shape", branches=1):
         """Prepare ``step_host``: the instances in ``groups`` groups contiguous in the state arena, of
         about equal state size (``groups`` = "shape": one group per instance shape), each with its
         own launch set, CUDA graph (``branches``: its graph branches, as in ``capture``) and
