@@ -251,3 +251,59 @@ def test_cheb_transform_2d_dealiased(pg, shape):
     assert rel_err(host(out2), sp2.dealias_forward(v)) < TOL
     assert L.pgx_cheb_transform_2d(ct.data_ptr(), M, 1, N, M, out.data_ptr(), Md, 1, Nd, Md, Nd, Md,
                                    _lib.DCT_BWD, work.data_ptr(), Nd * M - 1, st) == 1  # workspace too small
+
+
+def _dct_line_program(n, nlines, tb, nthreads, flags):
+    """LOAD -> forward DCT-I of n points -> STORE over ``nlines`` contiguous lines, through pgx_run
+    (the C ABI), with ``flags`` added to the DCT op's k; returns (input, output) on the host."""
+    import ctypes
+    import torch
+    from pypde_gb300 import _lib
+    L = _lib.lib()
+    x = torch.as_tensor(np.random.default_rng(n).uniform(-1, 1, (nlines, n)), device="cuda")
+    y = torch.full_like(x, 7.0)
+    tab = ctypes.c_void_p()
+    _lib.check(L.pgx_dct_table(n, ctypes.byref(tab)), "dct table")
+    P = _lib.PgxProgram()
+    P.axis, P.lines_len, P.tb, P.lcap, P.nslots, P.fft_n, P.nthreads = 1, 1, tb, (n + 1) | 1, 1, n, nthreads
+    ops = [_lib.op("LOAD", a=0, arr=0, len=0), _lib.op("DCT", a=0, b=1, mat=0, k=_lib.DCT_FWD | flags),
+           _lib.op("STORE", a=0, arr=1)]
+    P.nops = len(ops)
+    for i, o in enumerate(ops):
+        P.ops[i] = o
+    inst = _lib.PgxInstance()
+    for a, t in ((0, x), (1, y)):
+        inst.arr[a].ptr, inst.arr[a].s0, inst.arr[a].s1, inst.arr[a].n0, inst.arr[a].n1 = t.data_ptr(), n, 1, nlines, n
+    inst.len[0], inst.len[1] = n, nlines
+    inst.mat[0] = tab.value
+    _lib.check(L.pgx_run(ctypes.byref(P), ctypes.byref(inst), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "pgx_run")
+    torch.cuda.synchronize()
+    return host(x), host(y)
+
+
+@pytest.mark.parametrize("tb,nthreads", [(2, 64), (4, 32)])    # CTA-wide form, warp-local form
+@pytest.mark.parametrize("n", [9, 13, 17, 19, 33, 49, 97, 129])
+def test_in_slot_dct_matches_buffered_and_oracle(pg, n, tb, nthreads):
+    """PGX_DCT_SLOT (the FFT in the slot's own lines and the spare slot, the stage count made odd:
+    8 -> 2,2,2; 12 -> 3,2,2; 16 -> 4,2,2; 96 -> 3,4,2,2,2; 128 -> 4,4,2,2,2 points; 18, 32, 48 keep
+    theirs) gives the buffered transform to rounding and the oracle's forward Chebyshev transform."""
+    from oracle import spectral as sp
+    x, got = _dct_line_program(n, 6, tb, nthreads, _lib_flag("DCT_SLOT"))
+    _, ref = _dct_line_program(n, 6, tb, nthreads, 0)
+    assert rel_err(got, ref) < 1e-13
+    assert rel_err(got, sp.cheb_forward(x, axis=1)) < TOL
+
+
+@pytest.mark.parametrize("n", [7, 55])
+def test_in_slot_dct_refuses_lengths_without_an_odd_plan(pg, n):
+    """n - 1 = 2 * 3^b with b odd has no FFT plan with an odd number of stages: the in-slot transform
+    refuses (NaN outputs, no fault), the buffered one transforms."""
+    _, got = _dct_line_program(n, 6, 2, 64, _lib_flag("DCT_SLOT"))
+    _, ref = _dct_line_program(n, 6, 2, 64, 0)
+    assert np.isnan(got).all() and np.isfinite(ref).all()
+
+
+def _lib_flag(name):
+    from pypde_gb300 import _lib
+    return getattr(_lib, name)
