@@ -829,9 +829,9 @@ def main():
                     help="instance groups as parallel branches of the step's graph (0: tuned, -K: K "
                          "per instance shape)")
     ap.add_argument("--clocks-csv", default=None, help="where the nvidia-smi samples of the timed region go")
-    ap.add_argument("--e2e-groups", type=lambda v: v if v == "shape" else int(v), default="shape",
+    ap.add_argument("--e2e-groups", type=lambda v: v if v.startswith("shape") else int(v), default="shape",
                     help="instance groups of the end-to-end step, each on its own stream (a number, or "
-                         "'shape': one group per instance shape)")
+                         "'shape': one group per instance shape, 'shapeK': K per shape)")
     ap.add_argument("--split", default="auto", choices=["auto", "on", "off"],
                     help="per-field convection passes (auto: for batches of up to 4 instances)")
     ap.add_argument("--save-tiles", default=None)

@@ -1419,12 +1419,15 @@ class FusedBatch:
     def _split_groups(self, groups):
         """[(instance indices, first, end offset in state_arena)]: up to ``groups`` groups of
         instances contiguous in the arena and of about equal state size; ``groups`` = "shape": one
-        group per instance shape (contiguous: the arena is laid out by shape)."""
+        group per instance shape (contiguous: the arena is laid out by shape), "shapeK": K per shape."""
         order, starts = self._arena_order()
-        if groups == "shape":
-            cuts = [0] + [j for j in range(1, len(order))
+        if isinstance(groups, str) and groups.startswith("shape"):
+            # runs of one shape ("shapeK": each run in K contiguous parts of about equal counts)
+            per = int(groups[5:] or 1)
+            runs = [0] + [j for j in range(1, len(order))
                           if (self.insts[order[j]].N, self.insts[order[j]].M)
                           != (self.insts[order[j - 1]].N, self.insts[order[j - 1]].M)] + [len(order)]
+            cuts = sorted({a + (b - a) * q // per for a, b in zip(runs[:-1], runs[1:]) for q in range(per)} | {len(order)})
         else:
             cum = np.cumsum(np.diff(starts))
             cuts = [0] + [int(np.searchsorted(cum, cum[-1] * g / groups)) + 1 for g in range(1, groups)] + [len(cum)]

@@ -78,3 +78,23 @@ def test_shape_groups_follow_the_arena(seed):
         parts = fb._split_groups(groups)
         assert [i for r, _, _ in parts for i in r] == order       # arena order
         assert parts[0][1] == 0 and parts[-1][2] == fb.state_arena.numel()
+
+
+@pytest.mark.parametrize("per", [2, 3])
+def test_shape_groups_split_per_shape(per):
+    """"shapeK": every run of one shape in K contiguous groups of about equal instance counts."""
+    rng = np.random.default_rng(per)
+    shapes = [tuple(int(v) for v in s) for s in rng.choice([33, 65, 129], size=(40, 2))]
+    sizes = [5 * a * b for a, b in shapes]
+    order = sorted(range(len(shapes)), key=lambda k: shapes[k])
+    fb = fake_batch(sizes, order, shapes)
+    parts = fb._split_groups("shape%d" % per)
+    assert [i for r, _, _ in parts for i in r] == order
+    for shape in set(shapes):
+        counts = [len(r) for r, _, _ in parts if shapes[r[0]] == shape]
+        assert all(shapes[k] == shape for r, _, _ in parts if shapes[r[0]] == shape for k in r)
+        assert len(counts) == min(per, shapes.count(shape)) and max(counts) - min(counts) <= 1
+    end = 0
+    for r, o0, o1 in parts:
+        assert o0 == end and o1 - o0 == sum(sizes[k] for k in r)
+        end = o1
